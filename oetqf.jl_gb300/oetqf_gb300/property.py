@@ -1,0 +1,49 @@
+"""Fault and mantle properties, mirroring src/BEM/property.jl of Oetqf.jl."""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class RateStateQuasiDynamicProperty:
+    """Regularized rate-and-state friction with radiation damping (property.jl:10-25)."""
+
+    a: np.ndarray
+    b: np.ndarray
+    L: np.ndarray
+    σ: np.ndarray
+    η: float
+    vpl: float
+    f0: float = 0.6
+    v0: float = 1e-6
+
+    def __post_init__(self):
+        self.a, self.b, self.L, self.σ = (np.asarray(v, dtype=np.float64) for v in (self.a, self.b, self.L, self.σ))
+        assert self.a.shape == self.b.shape == self.L.shape == self.σ.shape
+        assert self.f0 > 0
+        assert self.v0 > 0
+        assert self.η > 0
+        assert self.vpl > 0
+
+
+@dataclass
+class PowerLawViscosityProperty:
+    """dϵ/dt = γ σ' τⁿ with ``n`` = power - 1 (property.jl:34-41, equation.jl:285)."""
+
+    γ: np.ndarray
+    n: np.ndarray
+    dϵ0: np.ndarray = field(default_factory=lambda: np.zeros(6))
+
+    def __post_init__(self):
+        self.γ = np.asarray(self.γ, dtype=np.float64)
+        self.n = np.asarray(self.n, dtype=np.float64)
+        self.dϵ0 = np.asarray(self.dϵ0, dtype=np.float64)
+        assert len(self.dϵ0) == 6
+        assert len(self.γ) == len(self.n)
+
+
+def dϵ_dt(p: PowerLawViscosityProperty, i: int, σ: float, τ: float) -> float:
+    """The viscosity law of src/BEM/equation.jl:285."""
+    return p.γ[i] * σ * τ ** p.n[i]

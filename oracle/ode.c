@@ -1,0 +1,247 @@
+/*
+ * Oracle: the ODE right-hand sides of src/BEM/equation.jl and an adaptive Tsit5 integrator
+ * standing in for the reference's OrdinaryDiffEq caller.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker for the CUDA path, and the timed CPU baseline; never
+ * linked into the product).
+ *
+ * The fault-fault traction rate is computed as the reference does it (equation.jl:44-61): a real
+ * DFT of the zero-padded v - vpl along strike (length 2nx-1), a per-frequency complex
+ * multiply-accumulate with the rFFT'd kernel, and the inverse real DFT truncated to nx rows. The
+ * DFT is the direct O(n^2) sum with tabulated twiddles (FFTW is not available here).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include "gbc_oracle.h"
+
+typedef struct { int n; double *cs, *sn; } twiddle;
+static _Thread_local twiddle tw = {0, NULL, NULL};
+
+static void tw_get(int n) {
+    if (tw.n == n) return;
+    free(tw.cs); free(tw.sn);
+    tw.cs = (double*)malloc(sizeof(double) * n);
+    tw.sn = (double*)malloc(sizeof(double) * n);
+    for (int m = 0; m < n; ++m) { tw.cs[m] = cos(2.0 * M_PI * m / n); tw.sn[m] = sin(2.0 * M_PI * m / n); }
+    tw.n = n;
+}
+
+/* relative_velocity! + dtau_dt! (equation.jl:35-61): dtau (nx,nxi) from v */
+void orc_dtau_dt(const orc_model* m, const double* v, double* dtau) {
+    const int nx = m->nx, nxi = m->nxi, n = 2 * nx - 1;
+    tw_get(n);
+    double* X = (double*)malloc(sizeof(double) * 2 * nx * nxi);   /* relv_dft (nx,nxi) complex */
+    double* Y = (double*)calloc(2 * (size_t)nx * nxi, sizeof(double)); /* dtau_dft */
+    for (int l = 0; l < nxi; ++l)
+        for (int k = 0; k < nx; ++k) {
+            double re = 0.0, im = 0.0;
+            for (int r = 0; r < nx; ++r) {
+                double val = v[r + nx * l] - m->vpl;
+                int idx = (int)(((long long)k * r) % n);
+                re += val * tw.cs[idx];
+                im -= val * tw.sn[idx];
+            }
+            X[2 * (k + nx * l)] = re;
+            X[2 * (k + nx * l) + 1] = im;
+        }
+    for (int j = 0; j < nxi; ++j)
+        for (int l = 0; l < nxi; ++l)
+            for (int k = 0; k < nx; ++k) {
+                const double* g = m->gf11_dft + 2 * ((size_t)k + (size_t)nx * (j + (size_t)nxi * l));
+                const double* x = X + 2 * (k + nx * l);
+                double* y = Y + 2 * (k + nx * j);
+                y[0] += g[0] * x[0] - g[1] * x[1];
+                y[1] += g[0] * x[1] + g[1] * x[0];
+            }
+    for (int j = 0; j < nxi; ++j)
+        for (int r = 0; r < nx; ++r) {
+            double acc = Y[2 * (nx * j)];
+            for (int k = 1; k < nx; ++k) {
+                int idx = (int)(((long long)k * r) % n);
+                const double* y = Y + 2 * (k + nx * j);
+                acc += 2.0 * (y[0] * tw.cs[idx] - y[1] * tw.sn[idx]);
+            }
+            dtau[r + nx * j] = acc / n;
+        }
+    free(X);
+    free(Y);
+}
+
+/* update_fault! with the ageing law (equation.jl:233-246, :279) */
+static void update_fault(const orc_model* m, const double* dtau, const double* v, const double* th,
+                         double* dv, double* dth, double* ddelta) {
+    const int N = m->nx * m->nxi;
+    for (int i = 0; i < N; ++i) {
+        double psi1 = exp((m->f0 + m->b[i] * log(m->v0 * fmax(0.0, th[i]) / m->L[i])) / m->a[i]) / (2.0 * m->v0);
+        double psi2 = m->sigma[i] * psi1 / hypot(1.0, v[i] * psi1);
+        double dmu_dv = m->a[i] * psi2;
+        double dmu_dth = m->b[i] / th[i] * v[i] * psi2;
+        dth[i] = 1.0 - v[i] * th[i] / m->L[i];
+        dv[i] = (dtau[i] - dmu_dth * dth[i]) / (dmu_dv + m->eta);
+        ddelta[i] = v[i];
+    }
+}
+
+void orc_ode_fault(const orc_model* m, const double* v, const double* th, double* dv, double* dth,
+                   double* ddelta) {
+    const int N = m->nx * m->nxi;
+    double* dtau = (double*)malloc(sizeof(double) * N);
+    orc_dtau_dt(m, v, dtau);
+    update_fault(m, dtau, v, th, dv, dth, ddelta);
+    free(dtau);
+}
+
+/* y (+)= A x for column-major A (rows x cols); rows split across threads */
+static void gemv_cm(const double* A, size_t rows, size_t cols, const double* x, double* y, int accumulate) {
+    const size_t B = 512;
+    const long nb = (long)((rows + B - 1) / B);
+#pragma omp parallel for schedule(static)
+    for (long bi = 0; bi < nb; ++bi) {
+        size_t r0 = (size_t)bi * B, r1 = r0 + B < rows ? r0 + B : rows;
+        double acc[512];
+        for (size_t r = r0; r < r1; ++r) acc[r - r0] = accumulate ? y[r] : 0.0;
+        for (size_t c = 0; c < cols; ++c) {
+            const double xc = x[c];
+            const double* a = A + rows * c;
+            for (size_t r = r0; r < r1; ++r) acc[r - r0] += a[r] * xc;
+        }
+        for (size_t r = r0; r < r1; ++r) y[r] = acc[r - r0];
+    }
+}
+
+void orc_ode_visco(const orc_model* m, const double* v, const double* th, const double* sig,
+                   double* dv, double* dth, double* deps, double* dsig, double* ddelta) {
+    const int N = m->nx * m->nxi, ne = m->ne;
+    double* dtau = (double*)malloc(sizeof(double) * N);
+    double* relv = (double*)malloc(sizeof(double) * N);
+    double* reldeps = (double*)malloc(sizeof(double) * 6 * (size_t)ne);
+    for (int i = 0; i < N; ++i) relv[i] = v[i] - m->vpl;
+    /* update_strain_rate! (equation.jl:207-222) with the power law dϵ = γ σ' τ^n (:285) */
+    for (int i = 0; i < ne; ++i) {
+        const double* s = sig;
+        double skk = (s[i] + s[i + 3 * ne] + s[i + 5 * ne]) / 3.0;
+        double sxx = s[i] - skk, syy = s[i + 3 * ne] - skk, szz = s[i + 5 * ne] - skk;
+        double sxy = s[i + ne], sxz = s[i + 2 * ne], syz = s[i + 4 * ne];
+        double tau = sqrt(sxx * sxx + syy * syy + szz * szz + 2.0 * (sxy * sxy + sxz * sxz + syz * syz));
+        double f = m->gamma[i] * pow(tau, m->n[i]);
+        deps[i] = f * sxx;
+        deps[i + ne] = f * sxy;
+        deps[i + 2 * ne] = f * sxz;
+        deps[i + 3 * ne] = f * syy;
+        deps[i + 4 * ne] = f * syz;
+        deps[i + 5 * ne] = f * szz;
+    }
+    /* relative_strain_rate! (:224-230) */
+    for (int k = 0; k < 6; ++k)
+        for (int i = 0; i < ne; ++i) reldeps[i + k * ne] = deps[i + k * ne] - m->deps0[k];
+    orc_dtau_dt(m, v, dtau);                                        /* :200 */
+    gemv_cm(m->gf21, N, 6 * (size_t)ne, reldeps, dtau, 1);          /* :201 */
+    gemv_cm(m->gf12, 6 * (size_t)ne, N, relv, dsig, 0);             /* :202 */
+    gemv_cm(m->gf22, 6 * (size_t)ne, 6 * (size_t)ne, reldeps, dsig, 1); /* :203 */
+    update_fault(m, dtau, v, th, dv, dth, ddelta);                  /* :204 */
+    free(dtau); free(relv); free(reldeps);
+}
+
+long long orc_state_len(const orc_model* m, int mantle) {
+    long long N = (long long)m->nx * m->nxi;
+    return mantle ? 3 * N + 12LL * m->ne : 3 * N;
+}
+
+static void rhs_flat(const orc_model* m, int mantle, const double* u, double* du) {
+    const long long N = (long long)m->nx * m->nxi;
+    if (!mantle) {
+        orc_ode_fault(m, u, u + N, du, du + N, du + 2 * N);
+    } else {
+        const long long E = 6LL * m->ne;
+        orc_ode_visco(m, u, u + N, u + 2 * N + E, du, du + N, du + 2 * N, du + 2 * N + E,
+                      du + 2 * N + 2 * E);
+    }
+}
+
+/* Tsitouras (2011) 5(4) tableau (order conditions verified by tests/test_oracle_ode.py). The
+ * right-hand side is autonomous, so the stage abscissae c_i are not needed here. */
+static const double TA[7][6] = {
+    {0},
+    {0.161},
+    {-0.008480655492356989, 0.335480655492357},
+    {2.897153057105493, -6.359448489975075, 4.3622954328695815},
+    {5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525},
+    {5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383},
+    {0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081, 2.324710524099774}};
+static const double TE[7] = {-0.00178001105222577714, -0.0008164344596567469, 0.007880878010261995,
+                             -0.1447110071732629, 0.5823571654525552, -0.45808210592918697,
+                             0.015151515151515152};
+
+void orc_tsit5_tableau(double a[7][6], double e[7]) {
+    memcpy(a, TA, sizeof(TA));
+    memcpy(e, TE, sizeof(TE));
+}
+
+int orc_integrate(const orc_model* m, double* u, double t0, double t1, const orc_solver_opts* o,
+                  orc_solver_stats* stt) {
+    const long long n = orc_state_len(m, o->mantle);
+    double* k[7];
+    for (int s = 0; s < 7; ++s) k[s] = (double*)malloc(sizeof(double) * n);
+    double* y = (double*)malloc(sizeof(double) * n);
+    double* un = (double*)malloc(sizeof(double) * n);
+    /* PI controller parameters for a 5th-order pair: beta2 = 2/(5*5), beta1 = 7*beta2/4 */
+    const double beta2 = 0.08, beta1 = 0.14, gam = 0.9, qmin = 0.2, qmax = 10.0;
+    double qold = 1e-4;
+    double t = t0, dt = o->dt0;
+    long long it = 0;
+    int status = 0;
+    memset(stt, 0, sizeof(*stt));
+    rhs_flat(m, o->mantle, u, k[0]);
+    stt->nrhs = 1;
+    while (t < t1) {
+        if (it++ >= o->maxiters) { status = -2; break; }
+        if (dt > o->dtmax) dt = o->dtmax;
+        if (t + dt > t1) dt = t1 - t;
+        for (int s = 1; s < 7; ++s) {
+            for (long long i = 0; i < n; ++i) {
+                double acc = 0.0;
+                for (int r = 0; r < s; ++r) acc += TA[s][r] * k[r][i];
+                y[i] = u[i] + dt * acc;
+            }
+            if (s == 6) memcpy(un, y, sizeof(double) * n);
+            rhs_flat(m, o->mantle, y, k[s]);
+        }
+        stt->nrhs += 6;
+        double ss = 0.0;
+        int finite = 1;
+        for (long long i = 0; i < n; ++i) {
+            double e = 0.0;
+            for (int s = 0; s < 7; ++s) e += TE[s] * k[s][i];
+            e *= dt;
+            double sc = o->abstol + o->reltol * fmax(fabs(u[i]), fabs(un[i]));
+            double r = e / sc;
+            ss += r * r;
+            if (!isfinite(un[i])) finite = 0;
+        }
+        double EEst = sqrt(ss / (double)n);
+        if (!finite || !isfinite(EEst)) EEst = INFINITY;
+        double q11 = pow(EEst, beta1);
+        if (EEst <= 1.0) {
+            double q = q11 / pow(qold, beta2);
+            q = fmax(1.0 / qmax, fmin(1.0 / qmin, q / gam));
+            t += dt;
+            memcpy(u, un, sizeof(double) * n);
+            double* tmp = k[0]; k[0] = k[6]; k[6] = tmp;   /* FSAL */
+            qold = fmax(EEst, 1e-4);
+            dt = dt / q;
+            stt->naccept++;
+        } else {
+            double q = isfinite(q11) ? fmin(1.0 / qmin, q11 / gam) : 1.0 / qmin;
+            dt = dt / q;
+            stt->nreject++;
+        }
+        if (dt < o->dtmin) { status = -1; break; }
+    }
+    stt->t = t;
+    stt->dt = dt;
+    stt->status = status;
+    for (int s = 0; s < 7; ++s) free(k[s]);
+    free(y); free(un);
+    return status;
+}

@@ -1,0 +1,119 @@
+"""The oracle's right-hand side and integrator against the reference's tests
+(test/BEM/tests.jl:63-110, :142-154) and published-method identities."""
+import numpy as np
+import pytest
+
+from oetqf_gb300.mesh import gen_hex8_box, gen_mesh
+from oetqf_gb300.property import PowerLawViscosityProperty, RateStateQuasiDynamicProperty, dϵ_dt
+
+
+def test_viscosity_law():
+    """test/BEM/tests.jl:142-149."""
+    rng = np.random.default_rng(0)
+    A, n, σ, τ = rng.random(4)
+    p = PowerLawViscosityProperty([A], [n], rng.random(6))
+    assert dϵ_dt(p, 0, σ, τ) == A * σ * τ ** n
+
+
+def test_tsit5_order_conditions(oracle):
+    a, e = oracle.tsit5_tableau()
+    A = np.zeros((7, 7))
+    for s in range(1, 7):
+        A[s, :s] = a[s, :s]
+    c = A.sum(axis=1)
+    b = A[6]
+    for k in range(5):
+        assert b @ c**k == pytest.approx(1 / (k + 1), abs=1e-13)
+    assert b @ A @ c == pytest.approx(1 / 6, abs=1e-13)
+    assert b @ A @ A @ c == pytest.approx(1 / 24, abs=1e-13)
+    assert (b * c) @ A @ c == pytest.approx(1 / 8, abs=1e-13)
+    bh = b - e
+    for k in range(4):
+        assert bh @ c**k == pytest.approx(1 / (k + 1), abs=1e-13)
+    assert e.sum() == pytest.approx(0.0, abs=1e-15)
+
+
+def _fault_model(oracle, seed=0, mesh=(10.0, 10.0, 2.0, 2.0, 90.0), buffer_ratio=1.0):
+    mf = gen_mesh("RectOkada", *mesh)
+    gf = oracle.gf_ff(mf, 1.0, 1.0, buffer_ratio=buffer_ratio, fourier=True)
+    rng = np.random.default_rng(seed)
+    p = RateStateQuasiDynamicProperty(*[rng.random((mf.nx, mf.nξ)) for _ in range(4)], *rng.random(4))
+    return mf, gf, p
+
+
+def test_okada_assemble_runs(oracle):
+    """test/BEM/tests.jl:63-71: the fault-only ode runs on random inputs."""
+    mf, gf, p = _fault_model(oracle)
+    m = oracle.OracleModel(gf, p)
+    u0 = np.random.default_rng(1).random(3 * mf.nx * mf.nξ)
+    du = m.ode(u0)
+    assert du.shape == u0.shape and np.all(np.isfinite(du))
+    np.testing.assert_array_equal(du[2 * mf.nx * mf.nξ:], u0[:mf.nx * mf.nξ])  # dδ = v
+
+
+def test_viscoelastic_assemble_runs(oracle):
+    """test/BEM/tests.jl:84-110 (gmsh box replaced by the structured box generator)."""
+    mf = gen_mesh("RectOkada", 100.0, 100.0, 10.0, 20.0, 90.0)
+    ma = gen_hex8_box(-100.0, -50.0, -20.0, 200.0, 100.0, -30.0, 2, 3, 4)
+    lam = mu = 1.0
+    gf11 = oracle.gf_ff(mf, lam, mu, fourier=True)
+    gf12 = oracle.gf_fm(mf, ma, lam, mu)
+    gf21 = oracle.gf_mf(ma, mf, lam, mu)
+    gf22 = oracle.gf_mm(ma, lam, mu)
+    rng = np.random.default_rng(2)
+    N, ne = mf.nx * mf.nξ, ma.ne
+    pf = RateStateQuasiDynamicProperty(*[rng.random((mf.nx, mf.nξ)) for _ in range(4)], *rng.random(4))
+    pa = PowerLawViscosityProperty(rng.random(ne), 3 * np.ones(ne), rng.random(6))
+    m = oracle.OracleModel(gf11, pf, gf12, gf21, gf22, pa)
+    u0 = np.concatenate([rng.random(N), rng.random(N), rng.random(6 * ne), rng.random(6 * ne), rng.random(N)])
+    du = m.ode(u0)
+    assert du.shape == u0.shape and np.all(np.isfinite(du))
+    # equation.jl:202-203 by hand
+    sig = u0[2 * N + 6 * ne:2 * N + 12 * ne].reshape((ne, 6), order="F")
+    skk = (sig[:, 0] + sig[:, 3] + sig[:, 5]) / 3
+    dev = sig.copy()
+    dev[:, [0, 3, 5]] -= skk[:, None]
+    tau = np.sqrt(dev[:, 0]**2 + dev[:, 3]**2 + dev[:, 5]**2 + 2 * (dev[:, 1]**2 + dev[:, 2]**2 + dev[:, 4]**2))
+    deps = pa.γ[:, None] * dev * tau[:, None] ** pa.n[:, None]
+    np.testing.assert_allclose(du[2 * N:2 * N + 6 * ne], deps.reshape(-1, order="F"), rtol=1e-13)
+    rel = (deps - pa.dϵ0[None, :]).reshape(-1, order="F")
+    dsig = gf12 @ (u0[:N] - pf.vpl) + gf22 @ rel
+    np.testing.assert_allclose(du[2 * N + 6 * ne:2 * N + 12 * ne], dsig, rtol=1e-10, atol=1e-12 * np.abs(dsig).max())
+
+
+def test_friction_formula(oracle):
+    """update_fault! (equation.jl:233-246) by hand on one model."""
+    mf, gf, p = _fault_model(oracle, seed=5)
+    m = oracle.OracleModel(gf, p)
+    N = mf.nx * mf.nξ
+    rng = np.random.default_rng(9)
+    v, th = rng.random(N), rng.random(N)
+    du = m.ode(np.concatenate([v, th, np.zeros(N)]))
+    dtau = m.dtau_dt(v.reshape((mf.nx, mf.nξ), order="F"))
+    a, b, L, s = (q.reshape(-1, order="F") for q in (p.a, p.b, p.L, p.σ))
+    psi1 = np.exp((p.f0 + b * np.log(p.v0 * np.maximum(0, th) / L)) / a) / (2 * p.v0)
+    psi2 = s * psi1 / np.hypot(1, v * psi1)
+    dth = 1 - v * th / L
+    dv = (dtau - b / th * v * psi2 * dth) / (a * psi2 + p.η)
+    np.testing.assert_allclose(du[N:2 * N], dth, rtol=1e-14)
+    np.testing.assert_allclose(du[:N], dv, rtol=1e-11)
+
+
+def test_integrator_matches_scipy(oracle):
+    """Tsit5 + PI control reproduces a tight scipy DOP853 solution of the same RHS."""
+    scipy_integrate = pytest.importorskip("scipy.integrate")
+    mf = gen_mesh("RectOkada", 8e3, 4e3, 1e3, 1e3, 90.0)
+    mu = 3e10
+    gf = oracle.gf_ff(mf, mu, mu, fourier=True)
+    N = mf.nx * mf.nξ
+    o = np.ones((mf.nx, mf.nξ))
+    vpl = 1e-9
+    p = RateStateQuasiDynamicProperty(0.015 * o, 0.019 * o, 0.012 * o, 5e7 * o, mu / (2 * 3044.0), vpl, 0.6, vpl)
+    m = oracle.OracleModel(gf, p)
+    th0 = 0.012 / vpl * (1 + 0.01 * np.linspace(-1, 1, N))
+    u0 = np.concatenate([np.full(N, vpl), th0, np.zeros(N)])
+    T = 3.15e7
+    u1, st = m.integrate(u0, 0.0, T, reltol=1e-10, abstol=1e-14, dt0=1e-3)
+    assert st.status == 0 and st.t == T
+    ref = scipy_integrate.solve_ivp(lambda t, y: m.ode(y), (0.0, T), u0, method="DOP853", rtol=1e-12, atol=1e-16)
+    np.testing.assert_allclose(u1, ref.y[:, -1], rtol=1e-7)
