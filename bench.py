@@ -1,0 +1,315 @@
+"""Benchmark: simulated years per second of an earthquake-cycle model on one GB300.
+
+Workload (default): a 100 km x 10 km vertical strike-slip fault at 1 km cells (1000 patches) over a
+Maxwell mantle from 10 to 30 km depth (50 x 10 x 5 = 2500 cells), FP64 Green's functions and
+arithmetic, integrated for 100 simulated years with Tsit5 (reltol 1e-6, abstol 1e-8, dt0 1e-8 s,
+dtmax 0.2 yr). Synthetic seeded inputs (splitmix64); the Green's functions are assembled on the
+device before timing.
+
+A bench "step" is one window of the horizon (horizon / K): warm-up integrates W short windows
+(0.01 yr each, from the initial state) untimed; the timed region integrates the K windows that
+cover the whole horizon. `value` keeps the state in HBM (gbc_integrate_dev); `e2e` repeats the
+horizon through the host-buffer C-ABI call gbc_integrate (state copied host->device and back every
+window). The RHS is read-bound on 2.04 GB of Green's functions, far above the 129 MB L2.
+
+--impl reference times the CPU oracle (the reference's algorithm restated in C with OpenMP; the
+Julia reference cannot run here) on the host cores. Under torchrun each rank integrates an
+independent replica (the path does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "oetqf.jl_gb300"))
+
+import numpy as np  # noqa: E402
+
+from oetqf_gb300.workloads import YEAR, strike_slip_fault, strike_slip_with_mantle  # noqa: E402
+
+SOLVER = dict(reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=0.2 * YEAR)
+# Tsit5 steps (accepted + rejected) this controller takes over each workload's horizon, as measured
+# by the device integrator (the CPU oracle's controller is the same and takes the same steps over
+# the horizons the parity tests cover); used to turn a bounded CPU sample into sim-yr/s.
+STEPS_FOR_HORIZON = {"fault-mantle-1000x2500-f64": 42388, "fault-800-f64": 4757}
+# DRAM bytes (read + write) of one k_rows launch from ncu, per workload
+# (profiles/k_rows_fault-mantle-1000x2500-f64.md)
+NCU_TRAFFIC = {"fault-mantle-1000x2500-f64": 2044237000 + 2987264}
+
+
+def workload(name):
+    if name == "fault-mantle-1000x2500-f64":
+        return strike_slip_with_mantle()
+    if name == "fault-800-f64":
+        return strike_slip_fault()
+    raise SystemExit(f"unknown workload {name}")
+
+
+def rhs_bytes(cm) -> int:
+    N, E = cm.N, 6 * cm.ne
+    gf = (E * (N + E) + N * E) * 8 + cm.mf.nx * cm.mf.nξ ** 2 * 8
+    state = (3 * N + 2 * E) * 8 * 2
+    return gf + state
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else ".",
+                                 f".clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200",
+                                          "-i", str(self.idx)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.remove(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return None, 0, 1
+    import torch.distributed as tdist
+    tdist.init_process_group("nccl" if os.environ.get("GBC_BENCH_BACKEND", "nccl") == "nccl" else "gloo")
+    return tdist, tdist.get_rank(), ws
+
+
+def cpu_oracle_model(cm, gfs=None):
+    """The workload on the FP64 oracle. With gfs=None (no GPU on this path) the mantle Green's
+    functions are stand-ins of the right shapes and scale: fault->mantle exact from the oracle,
+    mantle->fault from it by Betti/Mura reciprocity (area/volume weighted transpose), mantle-mantle
+    as its diagonal self-relaxation stored dense. The timed arithmetic -- dense FP64 GEMVs over
+    every entry plus the friction update -- does not depend on the values."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    gf11 = O.gf_ff(cm.mf, cm.lam, cm.mu, fourier=True)
+    if not cm.ne:
+        return O, O.OracleModel(gf11, cm.pf), "exact"
+    if gfs is not None:
+        return O, O.OracleModel(gf11, cm.pf, *gfs, cm.pa), "exact (exported from the device assembly)"
+    g12 = O.gf_fm(cm.mf, cm.ma, cm.lam, cm.mu)
+    vol = np.tile(cm.ma.Δx * cm.ma.Δy * cm.ma.Δz, 6) * np.repeat([1.0, 2, 2, 1, 2, 1], cm.ne)
+    area = cm.mf.Δx * cm.mf.Δξ
+    g21 = np.ascontiguousarray((g12 * vol[:, None]).T / area)
+    g22 = np.diag(np.full(6 * cm.ne, -cm.mu))
+    return O, O.OracleModel(gf11, cm.pf, g12, g21, g22, cm.pa), "stand-in mantle values (timing is value-independent)"
+
+
+def cpu_oracle_sample(cm, name, gfs=None, budget_s=20.0):
+    """Times the oracle's Tsit5 (all host threads) over a bounded number of steps of the full-size
+    workload and scales by the controller's step count for the whole horizon."""
+    O, om, how = cpu_oracle_model(cm, gfs)
+    t0 = time.perf_counter()
+    om.ode(cm.u0)
+    t_rhs = time.perf_counter() - t0
+    steps = int(min(500, max(3, budget_s / (6.0 * max(t_rhs, 1e-6)))))
+    t0 = time.perf_counter()
+    _, st = om.integrate(cm.u0, 0.0, cm.horizon, reltol=SOLVER["reltol"], abstol=SOLVER["abstol"], dt0=SOLVER["dt"],
+                         maxiters=steps)
+    wall = time.perf_counter() - t0
+    done = st.naccept + st.nreject
+    per_step = wall / max(done, 1)
+    total = per_step * STEPS_FOR_HORIZON[name]
+    return {"value": (cm.horizon / YEAR) / total, "unit": "sim-yr/s", "cores": O.num_threads(), "kind": "port",
+            "sample": f"{done} Tsit5 steps of the full-size workload on the C/OpenMP FP64 oracle "
+                      f"({per_step * 1e3:.2f} ms/step, Green's functions: {how}), scaled to the "
+                      f"{STEPS_FOR_HORIZON[name]} steps the same controller takes for {cm.horizon / YEAR:.0f} yr"}
+
+
+def run_reference(args):
+    tdist, rank, ws = dist()
+    if rank != 0:
+        return
+    cm = workload(args.workload)
+    vals = []
+    for _ in range(args.steps):
+        vals.append(cpu_oracle_sample(cm, args.workload, budget_s=args.cpu_budget / max(args.steps, 1)))
+    v = statistics.median([x["value"] for x in vals])
+    base = vals[0]
+    base["value"] = v
+    line = {"metric": "sim-yr/s", "value": v, "unit": "sim-yr/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": (cm.horizon / YEAR) / v / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded splitmix64)", "impl": "reference",
+            "config": {"workload": args.workload, "fault_patches": cm.N, "mantle_cells": cm.ne,
+                       "horizon_yr": cm.horizon / YEAR},
+            "cpu_baseline": base, "e2e": {"value": v, "unit": "sim-yr/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+    from oetqf_gb300 import _capi as C
+    from oetqf_gb300.equation import GB300Model
+
+    tdist, rank, ws = dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    cm = workload(args.workload)
+    if args.years:
+        cm.horizon = args.years * YEAR
+    H = cm.horizon
+    t_asm = time.perf_counter()
+    m = GB300Model(cm.mf.nx, cm.mf.nξ, cm.ne)
+    m.assemble_gf(cm.mf, cm.ma, cm.lam, cm.mu)
+    m.set_fault_props(cm.pf)
+    if cm.ne:
+        m.set_mantle_props(cm.pa)
+    t_asm = time.perf_counter() - t_asm
+    stream = torch.cuda.ExternalStream(m.stream)
+    u = torch.tensor(cm.u0, device="cuda")
+    if args.profile_rhs:
+        du = torch.zeros_like(u)
+        for _ in range(args.profile_rhs):
+            m.rhs_dev(u.data_ptr(), du.data_ptr())
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_rhs": args.profile_rhs, "assembly_s": t_asm}))
+        return
+    # warm-up: W short windows from the initial state
+    for _ in range(args.warmup):
+        u.copy_(torch.tensor(cm.u0, device="cuda"))
+        torch.cuda.synchronize()
+        m.integrate_dev(u.data_ptr(), 0.0, 0.01 * YEAR, **SOLVER)
+    u.copy_(torch.tensor(cm.u0, device="cuda"))
+    torch.cuda.synchronize()
+    K = args.steps
+    edges = np.linspace(0.0, H, K + 1)
+    clocks = Clocks(local)
+    clocks.start()
+    if tdist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = C.kernel_launches()
+    e0.record(stream)
+    naccept = nreject = 0
+    for k in range(K):
+        st = m.integrate_dev(u.data_ptr(), float(edges[k]), float(edges[k + 1]), **SOLVER)
+        if st.status != 0:
+            raise SystemExit(f"integration failed in window {k}: status {st.status}")
+        naccept += st.naccept
+        nreject += st.nreject
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    if tdist:
+        tdist.barrier()
+    ms = e0.elapsed_time(e1)
+    launches = C.kernel_launches() - launches0
+    clk = clocks.stop()
+    if tdist:
+        t = torch.tensor([ms], device="cuda")
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms = float(t.item())
+    sim_yr = H / YEAR
+    value = ws * sim_yr / (ms / 1e3)
+    # roofline of the dominant kernel (the row GEMV + friction launch): CUDA events on the model stream
+    du = torch.zeros_like(u)
+    R = 30
+    for _ in range(3):
+        m.rhs_dev(u.data_ptr(), du.data_ptr())
+    r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    r0.record(stream)
+    for _ in range(R):
+        m.rhs_dev(u.data_ptr(), du.data_ptr())
+    r1.record(stream)
+    r1.synchronize()
+    rhs_ms = r0.elapsed_time(r1) / R
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = rhs_bytes(cm) / (rhs_ms / 1e3) / 1e9
+    traffic = NCU_TRAFFIC.get(args.workload)
+    # e2e: the same horizon through the host-buffer C-ABI call (pinned host state, H2D + D2H per window)
+    uh = torch.tensor(cm.u0).pin_memory()
+    un = uh.numpy()
+    torch.cuda.synchronize()
+    x0, x1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    x0.record(stream)
+    for k in range(K):
+        out, st = m.integrate(un, float(edges[k]), float(edges[k + 1]), **SOLVER)
+        un[:] = out
+    x1.record(stream)
+    x1.synchronize()
+    e2e_ms = x0.elapsed_time(x1)
+    if rank != 0:
+        return
+    line = {"metric": "sim-yr/s", "value": value, "unit": "sim-yr/s", "n_gpus": ws, "steps": K, "warmup": args.warmup,
+            "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded splitmix64)",
+            "config": {"workload": args.workload, "fault_patches": cm.N, "mantle_cells": cm.ne, "horizon_yr": sim_yr,
+                       "precision": "f64", "solver": "Tsit5 reltol 1e-6 abstol 1e-8 dt0 1e-8 s dtmax 0.2 yr",
+                       "l2": "inputs larger than L2 (Green's functions read every RHS)", "parallelism": "replicas",
+                       "rk_steps": naccept + nreject, "rk_rejected": nreject, "assembly_s": round(t_asm, 3)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "kernel": "k_prologue + k_rows (one RHS)", "rhs_ms": rhs_ms,
+                         "bytes_per_launch": rhs_bytes(cm), "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"},
+            "e2e": {"value": sim_yr / (e2e_ms / 1e3), "unit": "sim-yr/s", "h2d_bytes_per_step": int(cm.u0.nbytes),
+                    "d2h_bytes_per_step": int(cm.u0.nbytes)},
+            "clocks": clk, "gpu_launches": launches}
+    if not args.no_cpu:
+        gfs = tuple(m.export_gf(w) for w in (C.GBC_GF12, C.GBC_GF21, C.GBC_GF22)) if cm.ne else None
+        line["cpu_baseline"] = cpu_oracle_sample(cm, args.workload, gfs=gfs, budget_s=args.cpu_budget)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbcycle", choices=["gbcycle", "reference"])
+    ap.add_argument("--workload", default="fault-mantle-1000x2500-f64", choices=list(STEPS_FOR_HORIZON))
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-rhs", type=int, default=0, help="run N right-hand sides only (for ncu captures)")
+    ap.add_argument("--years", type=float, default=0.0, help="override the horizon (profiling runs only)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

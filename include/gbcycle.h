@@ -1,0 +1,156 @@
+/*
+ * gbcycle -- C ABI of the GB300 earthquake-cycle hot path (libgbcycle.so).
+ *
+ * The library replaces, behind a plain C boundary, what the reference Oetqf.jl v0.3.6 computes
+ * on this path: the stress Green's functions (src/BEM/GF.jl) and the ODE right-hand side that
+ * OrdinaryDiffEq calls millions of times (src/BEM/equation.jl), plus an on-device adaptive
+ * integrator. Every entry point returns 0 on success or a negative GBC_E* code; the message of
+ * the last failure on the calling thread is available from gbc_last_error(). There is no CPU
+ * fallback: without a CUDA device every entry point that needs one fails with GBC_ENODEV.
+ *
+ * Arrays cross the boundary as plain pointers in the reference's Julia (column-major) layouts
+ * unless stated otherwise. "_dev" variants take device pointers (same CUDA context as the
+ * caller's, e.g. torch tensors on cuda:0) and run on the model's stream.
+ */
+#ifndef GBCYCLE_H
+#define GBCYCLE_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBC_OK 0
+#define GBC_EINVAL -1     /* bad argument (the reference raises AssertionError/ArgumentError) */
+#define GBC_ENODEV -2     /* no usable CUDA device */
+#define GBC_ECUDA -3      /* CUDA runtime error */
+#define GBC_ENOMEM -4     /* device allocation failed or HBM budget exceeded */
+#define GBC_ESOLVER -5    /* integration failed (dt below dtmin, maxiters, non-finite state) */
+#define GBC_ESTATE -6     /* model not ready (missing Green's functions or properties) */
+
+#define GBC_STRIKE_SLIP 0 /* StrikeSlip() (src/BEM/GF.jl:4) */
+#define GBC_DIP_SLIP 1    /* DipSlip()    (src/BEM/GF.jl:5) */
+
+/* RectOkadaMesh (src/BEM/mesh.jl:5-21). ax is (nx,2) and axi is (nxi,2), row-major (lo, hi). */
+typedef struct gbc_fault_mesh {
+    int nx, nxi;
+    const double *x, *xi, *y, *z;
+    const double *ax, *axi;
+    double dx, dxi, dep, dip;
+} gbc_fault_mesh;
+
+/* BEMHex8Mesh (src/BEM/mesh.jl:58-72); the rotation field is unused by the reference's GFs. */
+typedef struct gbc_hex_mesh {
+    int ne;
+    const double *cx, *cy, *cz, *qx, *qy, *qz, *dx, *dy, *dz;
+} gbc_hex_mesh;
+
+/* ---- Green's functions ------------------------------------------------------------------- */
+
+/* stress_greens_function(mesh::RectOkadaMesh, λ, μ; ftype, fourier, nrept, buffer_ratio)
+ * (src/BEM/GF.jl:31-71). out: real (nx,nxi,nxi) when fourier == 0, else complex interleaved
+ * (re,im) (nx,nxi,nxi) -- the rFFT of the circulant embedding (GF.jl:60-67). Host pointer. */
+int gbc_stress_gf_ff(const gbc_fault_mesh* mf, double lambda, double mu, int ftype, int fourier,
+                     int nrept, double buffer_ratio, double* out);
+
+/* stress_greens_function(mf, ma, λ, μ; ftype, qtype, nrept, buffer_ratio) (GF.jl:123-174).
+ * qcoords: 3*nq local coordinates in [-1,1]^3, qweights: nq normalised weights ("Gauss1" is
+ * one point at 0 with weight 1). out: (6ne, nx*nxi) column-major. Host pointer. */
+int gbc_stress_gf_fm(const gbc_fault_mesh* mf, const gbc_hex_mesh* ma, double lambda, double mu,
+                     int ftype, const double* qcoords, const double* qweights, int nq, int nrept,
+                     double buffer_ratio, double* out);
+
+/* stress_greens_function(ma, mf, λ, μ; ftype) (GF.jl:194-227). out: (nx*nxi, 6ne) col-major. */
+int gbc_stress_gf_mf(const gbc_hex_mesh* ma, const gbc_fault_mesh* mf, double lambda, double mu,
+                     int ftype, double* out);
+
+/* stress_greens_function(ma, λ, μ; qtype) (GF.jl:250-290, without the eigvals print).
+ * out: (6ne, 6ne) column-major. */
+int gbc_stress_gf_mm(const gbc_hex_mesh* ma, double lambda, double mu, const double* qcoords,
+                     const double* qweights, int nq, double* out);
+
+/* ---- Models: the ODEProblem parameter tuple of assemble (src/BEM/equation.jl:81-89,141-154) -- */
+
+typedef struct gbc_model gbc_model;
+
+#define GBC_PREC_F64 0    /* Green's functions stored and applied in FP64 */
+#define GBC_PREC_BF16 1   /* block-scaled BF16 storage (128x128 FP32 scales), FP32 accumulate */
+#define GBC_PREC_F16 2    /* block-scaled FP16 storage (128x128 FP32 scales), FP32 accumulate */
+
+/* A model with nx*nxi fault patches and ne mantle cells (ne = 0: fault-only, equation.jl:156-166;
+ * ne > 0: viscoelastic, equation.jl:185-205). Allocates device buffers; owns one CUDA stream. */
+int gbc_model_create(int nx, int nxi, int ne, gbc_model** out);
+void gbc_model_destroy(gbc_model* m);
+
+/* RateStateQuasiDynamicProperty (src/BEM/property.jl:10-25); a, b, L, sigma are (nx,nxi). */
+int gbc_model_set_fault_props(gbc_model* m, const double* a, const double* b, const double* L,
+                              const double* sigma, double eta, double vpl, double f0, double v0);
+/* PowerLawViscosityProperty (src/BEM/property.jl:34-41): gamma, n (= power - 1) of length ne and
+ * deps0 of length 6 (xx, xy, xz, yy, yz, zz). */
+int gbc_model_set_mantle_props(gbc_model* m, const double* gamma, const double* n,
+                               const double* deps0);
+
+#define GBC_GF11_REAL 0   /* (nx,nxi,nxi) real Toeplitz kernel */
+#define GBC_GF11_DFT 1    /* (nx,nxi,nxi) complex interleaved, the reference's fourier=true form */
+#define GBC_GF12 2        /* (6ne, N) fault -> mantle */
+#define GBC_GF21 3        /* (N, 6ne) mantle -> fault */
+#define GBC_GF22 4        /* (6ne, 6ne) mantle -> mantle */
+
+/* Upload a Green's function from host memory in the reference layout (the gf₁₁..gf₂₂ arguments
+ * of assemble, equation.jl:141-149). */
+int gbc_model_set_gf(gbc_model* m, int which, const double* host);
+/* Assemble every Green's function of the model directly on the device (no host round trip).
+ * ma may be NULL for a fault-only model. */
+int gbc_model_assemble(gbc_model* m, const gbc_fault_mesh* mf, const gbc_hex_mesh* ma,
+                       double lambda, double mu, int ftype, int nrept, double buffer_ratio,
+                       const double* qcoords, const double* qweights, int nq);
+/* Copy a Green's function back to host memory in the reference layout (parity checks). */
+int gbc_model_export_gf(gbc_model* m, int which, double* host);
+/* Storage precision of the mantle Green's functions (GBC_PREC_*); FP64 by default. */
+int gbc_model_set_precision(gbc_model* m, int mode);
+
+/* ode(du, u, p, t) (equation.jl:156-166 / 185-205) on host buffers in ArrayPartition order:
+ * nparts = 3: (v, θ, δ), each (nx,nxi); nparts = 5: (v, θ, ϵ, σ, δ), ϵ and σ (ne,6). */
+int gbc_rhs(gbc_model* m, double t, const double* const* u_parts, double* const* du_parts,
+            int nparts);
+/* Same on device memory: u and du are the flat concatenation of the parts (length
+ * gbc_model_state_len). Runs on the model's stream and does not synchronise. */
+int gbc_rhs_dev(gbc_model* m, double t, const double* u, double* du);
+long long gbc_model_state_len(const gbc_model* m);
+
+/* ---- On-device adaptive integration (stands in for OrdinaryDiffEq's solve, src/io.jl:125-130) */
+
+typedef struct gbc_solver_opts {
+    double reltol, abstol;   /* error norm: RMS of err / (abstol + reltol * max(|u|, |u_new|)) */
+    double dt0, dtmax, dtmin;
+    long long maxiters;
+} gbc_solver_opts;
+
+typedef struct gbc_solver_stats {
+    long long naccept, nreject, nrhs;
+    double t, dt;
+    int status;              /* 0 = reached t1, GBC_ESOLVER otherwise */
+} gbc_solver_stats;
+
+/* Tsit5 with PI step control from t0 to t1; u (flat, host) is overwritten with u(t1). */
+int gbc_integrate(gbc_model* m, double* u, double t0, double t1, const gbc_solver_opts* opts,
+                  gbc_solver_stats* stats);
+/* Same with the state already on the device; does not synchronise the stats until it returns. */
+int gbc_integrate_dev(gbc_model* m, double* u_dev, double t0, double t1,
+                      const gbc_solver_opts* opts, gbc_solver_stats* stats);
+
+/* The model's CUDA stream (a cudaStream_t), so callers can order their own work or record
+ * CUDA events around the library's launches. */
+void* gbc_model_stream(gbc_model* m);
+
+/* ---- Diagnostics ------------------------------------------------------------------------ */
+int gbc_last_error(char* buf, size_t len);
+const char* gbc_version(void);
+/* Number of kernels this library launched in this process (used to report GPU launch counts). */
+long long gbc_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

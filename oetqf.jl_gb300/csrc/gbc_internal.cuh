@@ -1,0 +1,58 @@
+// Internal declarations shared by the libgbcycle translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "gbcycle.h"
+
+namespace gbc {
+
+// thread-local last-error message, returned by gbc_last_error()
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define GBC_CUDA(call)                                       \
+    do {                                                     \
+        cudaError_t _e = (call);                             \
+        if (_e != cudaSuccess) return ::gbc::cuda_fail(_e, #call); \
+    } while (0)
+
+constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs (grids are sized from the live count)
+int sm_count();
+
+// Gauss-Legendre tables for the strain-volume stacks (4, 8, 12, 16 nodes), in constant memory.
+void gl_rule(int n, double* x, double* w);
+int upload_gl_tables();
+
+// ---- Green's-function assembly launches (gf_kernels.cu) -------------------------------------
+struct FaultDev {       // device copy of a fault mesh
+    int nx, nxi;
+    const double *x, *y, *z, *ax, *axi;  // ax: (nx,2) interleaved, axi: (nxi,2)
+    double dx, dep, dip;
+};
+struct HexDev {
+    int ne;
+    const double *cx, *cy, *cz, *qx, *qy, *qz, *dx, *dy, *dz;
+};
+// st (nx,nxi,nxi) column-major real Toeplitz kernel
+int launch_gf_ff(const FaultDev& f, double lambda, double mu, int ftype, int nrept,
+                 double buffer_ratio, double* st, cudaStream_t s);
+// rFFT of the circulant embedding, complex interleaved (nx,nxi,nxi)
+int launch_gf_ff_dft(int nx, int nxi, const double* st, double* st_dft, cudaStream_t s);
+// inverse: recover the real Toeplitz kernel from the reference's complex (nx,nxi,nxi) form
+int launch_gf_ff_idft(int nx, int nxi, const double* st_dft, double* st, cudaStream_t s);
+// fault -> mantle: rows (k*ne + i), cols j; written into a row-major matrix with leading dim ld
+int launch_gf_fm(const FaultDev& f, const HexDev& m, double lambda, double mu, int ftype,
+                 int nrept, double buffer_ratio, const double* qc, const double* qw, int nq,
+                 double* out, size_t ld, cudaStream_t s);
+// mantle -> fault: rows i (fault patch), cols (p*ne + j), row-major with leading dim ld
+int launch_gf_mf(const HexDev& m, const FaultDev& f, double lambda, double mu, int ftype,
+                 double* out, size_t ld, cudaStream_t s);
+// mantle-mantle: rows (k*ne + j), cols (p*ne + i), row-major with leading dim ld
+int launch_gf_mm(const HexDev& m, double lambda, double mu, const double* qc, const double* qw,
+                 int nq, double* out, size_t ld, cudaStream_t s);
+
+}  // namespace gbc

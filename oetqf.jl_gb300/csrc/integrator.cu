@@ -1,0 +1,231 @@
+// Device-resident Tsit5 (Tsitouras 2011, 5(4) pair) with a PI step-size controller, standing in
+// for the reference's OrdinaryDiffEq caller (src/io.jl:125-130, test/tests.jl:11).
+//
+// One step = 6 x (stage combination + RHS) + error norm/controller + commit, all on the device:
+// the controller kernel reads the error norm, accepts or rejects, and writes the next dt into
+// device memory, so steps chain without host round trips. The host captures a group of steps
+// into a CUDA graph and relaunches it until the controller reports completion; launches after
+// completion see Ctrl::done and return immediately.
+#include <cuda_runtime.h>
+
+#include "gbc_internal.cuh"
+#include "integrator.cuh"
+
+namespace gbc {
+
+__constant__ double c_ta[7][6] = {
+    {0},
+    {0.161},
+    {-0.008480655492356989, 0.335480655492357},
+    {2.897153057105493, -6.359448489975075, 4.3622954328695815},
+    {5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525},
+    {5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383},
+    {0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081, 2.324710524099774}};
+__constant__ double c_te[7] = {-0.00178001105222577714, -0.0008164344596567469, 0.007880878010261995,
+                               -0.1447110071732629, 0.5823571654525552, -0.45808210592918697,
+                               0.015151515151515152};
+
+struct KPtrs {
+    const double* k[7];
+};
+
+// y = u + dt * sum_{r < s} a[s][r] k_r
+__global__ void k_stage(int s, long long n, const double* __restrict__ u, KPtrs K, double* __restrict__ y,
+                        const Ctrl* __restrict__ c) {
+    if (c->done) return;
+    const double dt = c->dt;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int r = 0; r < s; ++r) acc = fma(c_ta[s][r], K.k[r][i], acc);
+        y[i] = u[i] + dt * acc;
+    }
+}
+
+// error norm partials, then the last block to finish runs the controller
+__global__ void k_error_control(long long n, const double* __restrict__ u, const double* __restrict__ un,
+                                KPtrs K, double* __restrict__ partial, Ctrl* c) {
+    if (c->done) return;
+    __shared__ double red[32];
+    __shared__ int last;
+    const double dt = c->dt, rtol = c->reltol, atol = c->abstol;
+    double ss = 0.0;
+    int bad = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double e = 0.0;
+#pragma unroll
+        for (int s = 0; s < 7; ++s) e = fma(c_te[s], K.k[s][i], e);
+        e *= dt;
+        const double unv = un[i];
+        const double sc = atol + rtol * fmax(fabs(u[i]), fabs(unv));
+        const double r = e / sc;
+        ss = fma(r, r, ss);
+        bad |= !isfinite(unv);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = bad ? INFINITY : ss;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += red[w];
+        partial[blockIdx.x] = b;
+        __threadfence();
+        const unsigned prev = atomicAdd(&c->blocks_done, 1u);
+        last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    double tot = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) tot += ((volatile double*)partial)[b];
+    c->blocks_done = 0;
+    double EEst = sqrt(tot / (double)n);
+    if (!isfinite(EEst)) EEst = INFINITY;
+    // PI controller for a 5th-order pair: beta1 = 7/50, beta2 = 2/25, safety 0.9, q in [1/10, 5]
+    const double beta1 = 0.14, beta2 = 0.08, gam = 0.9, qmin = 0.2, qmax = 10.0;
+    const double q11 = pow(EEst, beta1);
+    c->iters += 1;
+    c->nrhs += 6;
+    double dtn;
+    if (EEst <= 1.0) {
+        double q = q11 / pow(c->qold, beta2);
+        q = fmax(1.0 / qmax, fmin(1.0 / qmin, q / gam));
+        const double tn = c->t + dt;
+        c->t = (tn >= c->t1) ? c->t1 : tn;
+        c->qold = fmax(EEst, 1e-4);
+        c->naccept += 1;
+        c->accept = 1;
+        dtn = dt / q;
+    } else {
+        const double q = isfinite(q11) ? fmin(1.0 / qmin, q11 / gam) : 1.0 / qmin;
+        c->nreject += 1;
+        c->accept = 0;
+        dtn = dt / q;
+    }
+    if (c->t >= c->t1) {
+        c->done = 1;
+        c->status = 0;
+    } else if (dtn < c->dtmin || !isfinite(dtn)) {
+        c->done = 1;
+        c->status = -5;
+    } else if (c->iters >= c->maxiters) {
+        c->done = 1;
+        c->status = -5;
+    }
+    if (dtn > c->dtmax) dtn = c->dtmax;
+    const double rem = c->t1 - c->t;
+    if (dtn >= rem) dtn = rem;
+    c->dt = dtn;
+}
+
+// accept: u <- un and the FSAL derivative k0 <- k6
+__global__ void k_commit(long long n, double* __restrict__ u, const double* __restrict__ un, double* __restrict__ k0,
+                         const double* __restrict__ k6, const Ctrl* __restrict__ c) {
+    if (!c->accept) return;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        u[i] = un[i];
+        k0[i] = k6[i];
+    }
+}
+
+// the commit above must not run twice for one accepted step: clear the flag for the next step
+__global__ void k_clear_accept(Ctrl* c) { c->accept = 0; }
+
+int integrator_alloc(Integrator& I, long long n) {
+    if (I.n == n && I.y) return 0;
+    integrator_free(I);
+    I.n = n;
+    for (int s = 0; s < 7; ++s) GBC_CUDA(cudaMalloc(&I.k[s], sizeof(double) * n));
+    GBC_CUDA(cudaMalloc(&I.y, sizeof(double) * n));
+    GBC_CUDA(cudaMalloc(&I.un, sizeof(double) * n));
+    I.err_blocks = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 2);
+    if (I.err_blocks < 1) I.err_blocks = 1;
+    GBC_CUDA(cudaMalloc(&I.partial, sizeof(double) * I.err_blocks));
+    GBC_CUDA(cudaMalloc(&I.ctrl, sizeof(Ctrl)));
+    GBC_CUDA(cudaMallocHost(&I.ctrl_host, sizeof(Ctrl)));
+    return 0;
+}
+
+void integrator_free(Integrator& I) {
+    for (int s = 0; s < 7; ++s) if (I.k[s]) cudaFree(I.k[s]);
+    if (I.y) cudaFree(I.y);
+    if (I.un) cudaFree(I.un);
+    if (I.partial) cudaFree(I.partial);
+    if (I.ctrl) cudaFree(I.ctrl);
+    if (I.ctrl_host) cudaFreeHost(I.ctrl_host);
+    if (I.step_exec) cudaGraphExecDestroy(I.step_exec);
+    I = Integrator();
+}
+
+static int enqueue_step(Integrator& I, const RhsArgs& rhs0, double* u, cudaStream_t s) {
+    const long long n = I.n;
+    const int g = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 4);
+    RhsArgs rhs = rhs0;
+    rhs.skip = &I.ctrl->done;
+    KPtrs K;
+    for (int r = 0; r < 7; ++r) K.k[r] = I.k[r];
+    for (int st = 1; st < 7; ++st) {
+        double* dst = (st == 6) ? I.un : I.y;
+        k_stage<<<g, 256, 0, s>>>(st, n, u, K, dst, I.ctrl);
+        GBC_CUDA(cudaGetLastError());
+        if (int rc = launch_rhs(rhs, dst, I.k[st], s)) return rc;
+    }
+    k_error_control<<<I.err_blocks, 256, 0, s>>>(n, u, I.un, K, I.partial, I.ctrl);
+    GBC_CUDA(cudaGetLastError());
+    k_commit<<<g, 256, 0, s>>>(n, u, I.un, I.k[0], I.k[6], I.ctrl);
+    GBC_CUDA(cudaGetLastError());
+    k_clear_accept<<<1, 1, 0, s>>>(I.ctrl);
+    GBC_CUDA(cudaGetLastError());
+    return 0;
+}
+
+int integrator_run(Integrator& I, const RhsArgs& rhs0, double* u, double t0, double t1, double reltol,
+                   double abstol, double dt0, double dtmax, double dtmin, long long maxiters,
+                   cudaStream_t s) {
+    Ctrl h{};
+    h.t = t0;
+    h.t1 = t1;
+    h.dt = std::min(dt0, dtmax);
+    if (h.dt > t1 - t0) h.dt = t1 - t0;
+    h.qold = 1e-4;
+    h.reltol = reltol;
+    h.abstol = abstol;
+    h.dtmax = dtmax;
+    h.dtmin = dtmin;
+    h.maxiters = maxiters;
+    h.done = (t1 <= t0) ? 1 : 0;
+    *I.ctrl_host = h;
+    GBC_CUDA(cudaMemcpyAsync(I.ctrl, I.ctrl_host, sizeof(Ctrl), cudaMemcpyHostToDevice, s));
+    RhsArgs rhs = rhs0;
+    rhs.skip = nullptr;
+    if (int rc = launch_rhs(rhs, u, I.k[0], s)) return rc;  // FSAL seed k0 = f(u0)
+    // capture a group of steps once per (model, state pointer); relaunch until done
+    const int group = 8;
+    if (I.step_exec) {
+        cudaGraphExecDestroy(I.step_exec);
+        I.step_exec = nullptr;
+    }
+    cudaGraph_t graph;
+    GBC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc = 0;
+    for (int k = 0; k < group && rc == 0; ++k) rc = enqueue_step(I, rhs0, u, s);
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (rc) return rc;
+    GBC_CUDA(ce);
+    GBC_CUDA(cudaGraphInstantiate(&I.step_exec, graph, 0));
+    cudaGraphDestroy(graph);
+    I.steps_per_launch = group;
+    I.graph_launches = 0;
+    for (;;) {
+        GBC_CUDA(cudaGraphLaunch(I.step_exec, s));
+        ++I.graph_launches;
+        GBC_CUDA(cudaMemcpyAsync(I.ctrl_host, I.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
+        GBC_CUDA(cudaStreamSynchronize(s));
+        if (I.ctrl_host->done) break;
+    }
+    return I.ctrl_host->status;
+}
+
+}  // namespace gbc

@@ -1,0 +1,39 @@
+// Device-resident adaptive Tsit5 integration of one model.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "rhs.cuh"
+
+namespace gbc {
+
+// Solver state kept in device memory so whole steps run without the host.
+struct Ctrl {
+    double t, dt, t1, qold;
+    double reltol, abstol, dtmax, dtmin;
+    long long naccept, nreject, nrhs, iters, maxiters;
+    int done, status, accept, pad;
+    unsigned int blocks_done;
+};
+
+struct Integrator {
+    long long n = 0;
+    double* k[7] = {};   // stage derivatives
+    double* y = nullptr; // stage state
+    double* un = nullptr;
+    double* partial = nullptr;  // per-block error partial sums
+    Ctrl* ctrl = nullptr;       // device
+    Ctrl* ctrl_host = nullptr;  // pinned mirror
+    int err_blocks = 0;
+    cudaGraphExec_t step_exec = nullptr;  // captured group of steps
+    int steps_per_launch = 0;
+    long long graph_launches = 0;  // graph launches of the last run
+};
+
+int integrator_alloc(Integrator& I, long long n);
+void integrator_free(Integrator& I);
+// Integrates u (device) from t0 to t1. Fills the host mirror of Ctrl.
+int integrator_run(Integrator& I, const RhsArgs& rhs, double* u, double t0, double t1,
+                   double reltol, double abstol, double dt0, double dtmax, double dtmin,
+                   long long maxiters, cudaStream_t s);
+
+}  // namespace gbc

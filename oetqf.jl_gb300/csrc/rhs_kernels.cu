@@ -1,0 +1,136 @@
+// FP64 right-hand side on the device.
+//
+// Viscoelastic ode (equation.jl:185-205) as two launches:
+//   1. prologue, one thread per mantle cell / fault patch: update_strain_rate! (:207-222) writes
+//      dϵ into du, relative_strain_rate! (:224-230) and relative_velocity! (:35-42) fill the
+//      scratch vector x = [v - vpl; dϵ - dϵ₀];
+//   2. one warp per receiver row: mantle rows compute dσ = [G12 | G22] x (:202-203) as a single
+//      GEMV; fault rows compute the Toeplitz traction rate sum_{k,l} st[|i-k|, j, l] (v - vpl)[k,l]
+//      (the FFT convolution of :44-61 applied directly) plus G21 (dϵ - dϵ₀) (:201), then the
+//      friction epilogue update_fault! (:233-246) in the same warp.
+// Fault-only ode (:156-166) is the second launch alone, with v - vpl formed on the fly.
+// Each row's sum is reduced in a fixed order (lane partials, then a shuffle tree), so results
+// are bitwise reproducible run to run.
+#include <cuda_runtime.h>
+
+#include "gbc_internal.cuh"
+#include "rhs.cuh"
+
+namespace gbc {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// sum_c A[c] * x[c] over c in [0, n) by one warp; A and x 16-byte aligned
+__device__ __forceinline__ double warp_dot(const double* __restrict__ A, const double* __restrict__ x,
+                                           long long n, int lane) {
+    const double2* A2 = reinterpret_cast<const double2*>(A);
+    const double2* x2 = reinterpret_cast<const double2*>(x);
+    const long long n2 = n >> 1;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    long long c = lane;
+    for (; c + 32 < n2; c += 64) {
+        const double2 a0 = __ldcs(A2 + c), a1 = __ldcs(A2 + c + 32);
+        const double2 x0 = __ldg(x2 + c), x1 = __ldg(x2 + c + 32);
+        s0 = fma(a0.x, x0.x, s0);
+        s1 = fma(a0.y, x0.y, s1);
+        s2 = fma(a1.x, x1.x, s2);
+        s3 = fma(a1.y, x1.y, s3);
+    }
+    for (; c < n2; c += 32) {
+        const double2 a0 = __ldcs(A2 + c);
+        const double2 x0 = __ldg(x2 + c);
+        s0 = fma(a0.x, x0.x, s0);
+        s1 = fma(a0.y, x0.y, s1);
+    }
+    if ((n & 1) && lane == 0) s0 = fma(__ldcs(A + n - 1), __ldg(x + n - 1), s0);
+    return (s0 + s1) + (s2 + s3);
+}
+
+__global__ void k_prologue(RhsArgs a, const double* __restrict__ u, double* __restrict__ du,
+                           StateLayout L) {
+    if (a.skip && *a.skip) return;
+    const int ne = a.ne, N = a.N;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N + ne; t += gridDim.x * blockDim.x) {
+        if (t < N) {
+            a.xm[t] = u[L.v + t] - a.vpl;
+            continue;
+        }
+        const int i = t - N;
+        const double* s = u + L.sig;
+        const double skk = (s[i] + s[i + 3 * ne] + s[i + 5 * ne]) / 3.0;
+        const double sxx = s[i] - skk, syy = s[i + 3 * ne] - skk, szz = s[i + 5 * ne] - skk;
+        const double sxy = s[i + ne], sxz = s[i + 2 * ne], syz = s[i + 4 * ne];
+        const double tau = sqrt(sxx * sxx + syy * syy + szz * szz + 2.0 * (sxy * sxy + sxz * sxz + syz * syz));
+        const double f = a.gamma[i] * pow(tau, a.nexp[i]);
+        const double d[6] = {f * sxx, f * sxy, f * sxz, f * syy, f * syz, f * szz};
+        double* deps = du + L.eps;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            deps[i + k * ne] = d[k];
+            a.xm[a.npad + i + k * ne] = d[k] - a.deps0[k];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_rows(RhsArgs a, const double* __restrict__ u,
+                                              double* __restrict__ du, StateLayout L) {
+    if (a.skip && *a.skip) return;
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    const int N = a.N, nx = a.nx, nxi = a.nxi;
+    const long long M = 6LL * a.ne;
+    for (long long w = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); w < M + N; w += warps) {
+        if (w < M) {  // mantle stress-rate row
+            const double r = warp_sum(warp_dot(a.gm + w * a.ldm, a.xm, a.npad + M, lane));
+            if (lane == 0) du[L.sig + w] = r;
+            continue;
+        }
+        const int i = (int)(w - M), ii = i % nx, j = i / nx;
+        // fault-fault traction rate: symmetric block-Toeplitz sum
+        double acc = 0.0;
+        const double* v = u + L.v;
+        for (int m = lane; m < N; m += 32) {
+            const int k = m % nx, l = m / nx;
+            const int d = ii > k ? ii - k : k - ii;
+            acc = fma(__ldg(a.st + d + (size_t)nx * (j + (size_t)nxi * l)), v[m] - a.vpl, acc);
+        }
+        if (M > 0) acc += warp_dot(a.g21 + (size_t)i * a.ld21, a.xm + a.npad, M, lane);
+        const double dtau = warp_sum(acc);
+        if (lane == 0) {
+            const double vi = v[i], th = u[L.th + i];
+            const double ai = a.a[i], bi = a.b[i], Li = a.L[i];
+            const double psi1 = exp((a.f0 + bi * log(a.v0 * fmax(0.0, th) / Li)) / ai) / (2.0 * a.v0);
+            const double psi2 = a.sig[i] * psi1 / hypot(1.0, vi * psi1);
+            const double dmu_dv = ai * psi2;
+            const double dmu_dth = bi / th * vi * psi2;
+            const double dth = 1.0 - vi * th / Li;
+            du[L.th + i] = dth;
+            du[L.v + i] = (dtau - dmu_dth * dth) / (dmu_dv + a.eta);
+            du[L.delta + i] = vi;
+        }
+    }
+}
+
+int launch_rhs(const RhsArgs& a, const double* u, double* du, cudaStream_t s) {
+    const StateLayout L = layout_of(a.N, a.ne);
+    const int sms = sm_count();
+    if (a.ne > 0) {
+        const int n = a.N + a.ne;
+        int g = (n + 255) / 256;
+        if (g > sms * 8) g = sms * 8;
+        k_prologue<<<g, 256, 0, s>>>(a, u, du, L);
+        GBC_CUDA(cudaGetLastError());
+    }
+    const long long rows = 6LL * a.ne + a.N;
+    long long g = (rows + 7) / 8;
+    if (g > (long long)sms * 8) g = (long long)sms * 8;
+    k_rows<<<(int)g, 256, 0, s>>>(a, u, du, L);
+    GBC_CUDA(cudaGetLastError());
+    return 0;
+}
+
+}  // namespace gbc

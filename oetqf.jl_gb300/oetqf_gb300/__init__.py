@@ -1,0 +1,24 @@
+"""oetqf_gb300: the GB300 (sm_103a) earthquake-cycle hot path of Oetqf.jl behind a C ABI.
+
+Host-side mirror of the reference API: meshes (src/BEM/mesh.jl), properties
+(src/BEM/property.jl), stress_greens_function (src/BEM/GF.jl), assemble and the ODE right-hand
+side (src/BEM/equation.jl), and an on-device adaptive integrator. Compute runs in libgbcycle.so.
+"""
+from .mesh import (BEMHex8Mesh, RectOkadaMesh, gauss1_quadrature, gauss_product_quadrature, gen_hex8_box,
+                   gen_mesh, sincosd)
+from .property import PowerLawViscosityProperty, RateStateQuasiDynamicProperty, dϵ_dt
+
+__all__ = ["BEMHex8Mesh", "RectOkadaMesh", "gen_mesh", "gen_hex8_box", "gauss1_quadrature", "gauss_product_quadrature",
+           "sincosd", "RateStateQuasiDynamicProperty", "PowerLawViscosityProperty", "dϵ_dt", "stress_greens_function",
+           "StrikeSlip", "DipSlip", "assemble", "solve", "ArrayPartition", "GB300Model", "ODEProblem"]
+
+
+def __getattr__(name):
+    # GPU-facing pieces load libgbcycle.so lazily so mesh/property code works without a GPU
+    if name in ("stress_greens_function", "StrikeSlip", "DipSlip"):
+        from . import greens
+        return getattr(greens, name)
+    if name in ("assemble", "solve", "ArrayPartition", "GB300Model", "ODEProblem"):
+        from . import equation
+        return getattr(equation, name)
+    raise AttributeError(name)

@@ -1,0 +1,57 @@
+"""The C-ABI library without a GPU: it builds, loads, exports every symbol include/gbcycle.h
+declares, and fails loudly (no CPU fallback) when no device is present."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "gbcycle.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbc_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_the_boundary():
+    names = _declared()
+    for n in ("gbc_stress_gf_ff", "gbc_stress_gf_fm", "gbc_stress_gf_mf", "gbc_stress_gf_mm", "gbc_model_create",
+              "gbc_rhs", "gbc_rhs_dev", "gbc_integrate", "gbc_last_error"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol():
+    from oetqf_gb300 import _capi as C
+    L = C.lib()
+    for n in _declared():
+        assert hasattr(L, n), n
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the no-GPU error path")
+def test_no_cpu_fallback_without_gpu():
+    from oetqf_gb300 import _capi as C
+    h = ctypes.c_void_p()
+    rc = C.lib().gbc_model_create(4, 2, 0, ctypes.byref(h))
+    assert rc == -2 and not h.value
+    assert "no CUDA device" in C.last_error()
+    from oetqf_gb300 import gen_mesh, stress_greens_function
+    with pytest.raises(C.GbcError):
+        stress_greens_function(gen_mesh("RectOkada", 4.0, 2.0, 1.0, 1.0, 90.0), 1.0, 1.0)
+
+
+def test_invalid_arguments_rejected_before_device_use():
+    from oetqf_gb300 import _capi as C
+    h = ctypes.c_void_p()
+    assert C.lib().gbc_model_create(0, 2, 0, ctypes.byref(h)) == -1
+    assert C.lib().gbc_model_create(2, 2, -1, ctypes.byref(h)) == -1
