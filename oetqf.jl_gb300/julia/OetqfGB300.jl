@@ -1,0 +1,109 @@
+# Julia glue for libgbcycle.so: GB300 Green's functions and a drop-in ODE right-hand side for
+# Oetqf.jl. The reference's mesh, property and assemble API stays as it is; `assemble_gb300`
+# returns an ODEProblem{true} whose f(du, u, p, t) calls the CUDA RHS through ccall.
+# (Not exercised in this repository's tests: no Julia toolchain is available where they run.)
+module OetqfGB300
+
+using Oetqf, RecursiveArrayTools, OrdinaryDiffEq
+
+const libgbc = get(ENV, "GBCYCLE_LIB", joinpath(@__DIR__, "..", "lib", "libgbcycle.so"))
+
+struct GbcFaultMesh
+    nx::Cint; nxi::Cint
+    x::Ptr{Cdouble}; xi::Ptr{Cdouble}; y::Ptr{Cdouble}; z::Ptr{Cdouble}
+    ax::Ptr{Cdouble}; axi::Ptr{Cdouble}
+    dx::Cdouble; dxi::Cdouble; dep::Cdouble; dip::Cdouble
+end
+
+struct GbcHexMesh
+    ne::Cint
+    cx::Ptr{Cdouble}; cy::Ptr{Cdouble}; cz::Ptr{Cdouble}
+    qx::Ptr{Cdouble}; qy::Ptr{Cdouble}; qz::Ptr{Cdouble}
+    dx::Ptr{Cdouble}; dy::Ptr{Cdouble}; dz::Ptr{Cdouble}
+end
+
+function check(rc)
+    rc == 0 && return
+    buf = Vector{UInt8}(undef, 1024)
+    ccall((:gbc_last_error, libgbc), Cint, (Ptr{UInt8}, Csize_t), buf, length(buf))
+    throw(ErrorException("gbcycle error $rc: " * unsafe_string(pointer(buf))))
+end
+
+pairs_rowmajor(a) = collect(Iterators.flatten(a))   # Vector{NTuple{2}} -> (n,2) row-major
+
+"GPU stress_greens_function(mesh::RectOkadaMesh, λ, μ; ...) (src/BEM/GF.jl:31)."
+function stress_greens_function_gb300(mf::RectOkadaMesh, λ::Float64, μ::Float64;
+        ftype=StrikeSlip(), fourier::Bool=true, nrept::Integer=2, buffer_ratio::Real=0)
+    ax, axi = pairs_rowmajor(mf.ax), pairs_rowmajor(mf.aξ)
+    GC.@preserve mf ax axi begin
+        m = GbcFaultMesh(mf.nx, mf.nξ, pointer(mf.x), pointer(mf.ξ), pointer(mf.y), pointer(mf.z),
+                         pointer(ax), pointer(axi), mf.Δx, mf.Δξ, mf.dep, mf.dip)
+        out = fourier ? Array{ComplexF64}(undef, mf.nx, mf.nξ, mf.nξ) : Array{Float64}(undef, mf.nx, mf.nξ, mf.nξ)
+        check(ccall((:gbc_stress_gf_ff, libgbc), Cint,
+                    (Ref{GbcFaultMesh}, Cdouble, Cdouble, Cint, Cint, Cint, Cdouble, Ptr{Cvoid}),
+                    m, λ, μ, ftype isa StrikeSlip ? 0 : 1, fourier, nrept, buffer_ratio, out))
+    end
+    return out
+end
+
+mutable struct GB300Model
+    h::Ptr{Cvoid}
+    nx::Int; nξ::Int; ne::Int
+end
+
+function GB300Model(nx, nξ, ne=0)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:gbc_model_create, libgbc), Cint, (Cint, Cint, Cint, Ref{Ptr{Cvoid}}), nx, nξ, ne, h))
+    m = GB300Model(h[], nx, nξ, ne)
+    finalizer(x -> ccall((:gbc_model_destroy, libgbc), Cvoid, (Ptr{Cvoid},), x.h), m)
+    return m
+end
+
+set_gf!(m::GB300Model, which::Integer, gf::AbstractArray) =
+    check(ccall((:gbc_model_set_gf, libgbc), Cint, (Ptr{Cvoid}, Cint, Ptr{Cvoid}), m.h, which, gf))
+
+function set_props!(m::GB300Model, p::RateStateQuasiDynamicProperty)
+    check(ccall((:gbc_model_set_fault_props, libgbc), Cint,
+                (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Cdouble, Cdouble, Cdouble, Cdouble),
+                m.h, p.a, p.b, p.L, p.σ, p.η, p.vpl, p.f₀, p.v₀))
+end
+
+function set_props!(m::GB300Model, p::PowerLawViscosityProperty)
+    check(ccall((:gbc_model_set_mantle_props, libgbc), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
+                m.h, Vector{Float64}(p.γ), Vector{Float64}(p.n), Vector{Float64}(p.dϵ₀)))
+end
+
+"The drop-in derivative: OrdinaryDiffEq calls f(du, u, p, t) in place; u and du are ArrayPartitions."
+function gpu_ode(du::ArrayPartition, u::ArrayPartition, m::GB300Model, t)
+    n = length(u.x)
+    up = Ptr{Cdouble}[pointer(x) for x in u.x]
+    dp = Ptr{Cdouble}[pointer(x) for x in du.x]
+    GC.@preserve u du up dp begin
+        check(ccall((:gbc_rhs, libgbc), Cint, (Ptr{Cvoid}, Cdouble, Ptr{Ptr{Cdouble}}, Ptr{Ptr{Cdouble}}, Cint),
+                    m.h, t, up, dp, n))
+    end
+    return nothing
+end
+
+"assemble(gf, p, u0, tspan) with the RHS on the GB300 (src/BEM/equation.jl:81-89)."
+function assemble_gb300(gf::AbstractArray, p::RateStateQuasiDynamicProperty, u0::ArrayPartition, tspan::NTuple{2})
+    nx, nξ = size(u0.x[1])
+    m = GB300Model(nx, nξ, 0)
+    set_gf!(m, eltype(gf) <: Complex ? 1 : 0, gf)
+    set_props!(m, p)
+    return ODEProblem{true}(gpu_ode, u0, tspan, m)
+end
+
+"assemble(gf₁₁, gf₁₂, gf₂₁, gf₂₂, pf, pa, u0, tspan) with the RHS on the GB300 (equation.jl:141-154)."
+function assemble_gb300(gf₁₁::AbstractArray, gf₁₂::AbstractMatrix, gf₂₁::AbstractMatrix, gf₂₂::AbstractMatrix,
+                        pf::RateStateQuasiDynamicProperty, pa::PowerLawViscosityProperty,
+                        u0::ArrayPartition, tspan::NTuple{2})
+    nx, nξ = size(u0.x[1]); ne = size(u0.x[3], 1)
+    m = GB300Model(nx, nξ, ne)
+    set_gf!(m, eltype(gf₁₁) <: Complex ? 1 : 0, gf₁₁)
+    set_gf!(m, 2, gf₁₂); set_gf!(m, 3, gf₂₁); set_gf!(m, 4, gf₂₂)
+    set_props!(m, pf); set_props!(m, pa)
+    return ODEProblem{true}(gpu_ode, u0, tspan, m)
+end
+
+end # module
