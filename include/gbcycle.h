@@ -140,6 +140,27 @@ int gbc_integrate(gbc_model* m, double* u, double t0, double t1, const gbc_solve
 int gbc_integrate_dev(gbc_model* m, double* u_dev, double t0, double t1,
                       const gbc_solver_opts* opts, gbc_solver_stats* stats);
 
+/* Viscoelastic ode(du, u, p, t) (equation.jl:185-205) that allocates no device memory. No
+ * counterpart in the reference: it is for callers that cannot call cudaMalloc when they evaluate
+ * the right-hand side -- code running while another library captures the stream into a CUDA
+ * graph (allocation is not permitted during capture), processes whose device memory is owned by
+ * their own pool, and bindings that only pass raw device pointers. Every input and output is the
+ * caller's device memory (deps0 excepted: 6 doubles in host memory):
+ *   st (nx,nxi,nxi) real Toeplitz kernel, column-major;
+ *   gm row-major (6ne rows, leading dim ldm >= npad + 6ne, even): columns [0,N) hold G12,
+ *      [N,npad) zeros and [npad, npad+6ne) G22, with N = nx*nxi and npad = N rounded up to 32;
+ *   g21 row-major (N rows, leading dim ld21 >= 6ne, even);
+ *   a, b, L, sigma (N), gamma, n (ne); u, du flat states of length 3N + 12ne.
+ * The one scratch vector lives in a fixed 8 MiB device array inside the library, so the model
+ * must satisfy npad + 6ne <= 1048576 (GBC_EINVAL otherwise). The first call on each device looks
+ * the array up (and may load the library's device code): make it before any stream capture.
+ * All calls share the array: calls whose work overlaps on the GPU race. stream may be NULL. */
+int gbc_rhs_visco_noalloc(int nx, int nxi, int ne, const double* st, const double* gm, size_t ldm,
+                          const double* g21, size_t ld21, const double* a, const double* b,
+                          const double* L, const double* sigma, double eta, double vpl, double f0,
+                          double v0, const double* gamma, const double* n, const double* deps0,
+                          const double* u, double* du, void* stream);
+
 /* The model's CUDA stream (a cudaStream_t), so callers can order their own work or record
  * CUDA events around the library's launches. */
 void* gbc_model_stream(gbc_model* m);

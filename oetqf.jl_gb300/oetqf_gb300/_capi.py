@@ -80,6 +80,9 @@ def lib():
         L.gbc_model_state_len.argtypes = [P]
         L.gbc_model_state_len.restype = LL
         L.gbc_kernel_launches.restype = LL
+        L.gbc_rhs_visco_noalloc.argtypes = [I, I, I, P, P, ctypes.c_size_t, P, ctypes.c_size_t, P, P, P, P, D, D, D, D,
+                                            P, P, PD, P, P, P]
+        L.gbc_rhs_visco_noalloc.restype = I
         L.gbc_model_stream.argtypes = [P]
         L.gbc_model_stream.restype = P
         L.gbc_version.restype = ctypes.c_char_p
