@@ -107,8 +107,16 @@ int gbc_model_assemble(gbc_model* m, const gbc_fault_mesh* mf, const gbc_hex_mes
                        const double* qcoords, const double* qweights, int nq);
 /* Copy a Green's function back to host memory in the reference layout (parity checks). */
 int gbc_model_export_gf(gbc_model* m, int which, double* host);
-/* Storage precision of the mantle Green's functions (GBC_PREC_*); FP64 by default. */
+/* Storage precision of the mantle Green's functions (GBC_PREC_*); FP64 by default. BF16/FP16
+ * store [G12|G22] and G21 as one 16-bit matrix with an FP32 scale per 128x128 block and
+ * accumulate in FP32; the fault-fault kernel runs in FP32 and friction stays FP64. The 16-bit
+ * copy is rebuilt from the FP64 Green's functions whenever they change. */
 int gbc_model_set_precision(gbc_model* m, int mode);
+/* Integrate ψ = ln θ instead of θ inside gbc_integrate* (the caller's state keeps θ). */
+int gbc_model_set_log_theta(gbc_model* m, int on);
+/* Device error word of the model's bounded waits (0 = none); nonzero means a TMA pipeline wait
+ * timed out and the last right-hand side is not valid. */
+int gbc_model_error_word(gbc_model* m);
 
 /* ode(du, u, p, t) (equation.jl:156-166 / 185-205) on host buffers in ArrayPartition order:
  * nparts = 3: (v, θ, δ), each (nx,nxi); nparts = 5: (v, θ, ϵ, σ, δ), ϵ and σ (ne,6). */

@@ -65,6 +65,26 @@ struct DevBuf {
     ~DevBuf() { release(); }
 };
 
+struct RawBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    int alloc(size_t nbytes) {
+        if (p && bytes == nbytes) return 0;
+        release();
+        if (nbytes == 0) return 0;
+        cudaError_t e = cudaMalloc(&p, nbytes);
+        if (e != cudaSuccess) { p = nullptr; return cuda_fail(e, "cudaMalloc"); }
+        bytes = nbytes;
+        return 0;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    ~RawBuf() { release(); }
+};
+
 static int upload(DevBuf& b, const double* h, size_t count, cudaStream_t s) {
     if (int rc = b.alloc(count)) return rc;
     GBC_CUDA(cudaMemcpyAsync(b.p, h, sizeof(double) * count, cudaMemcpyHostToDevice, s));
@@ -132,6 +152,11 @@ struct gbc_model {
     double eta = 0, vpl = 0, f0 = 0.6, v0 = 1e-6, deps0[6] = {0, 0, 0, 0, 0, 0};
     bool props = false, mprops = false, has_st = false, has_g12 = false, has_g21 = false, has_g22 = false;
     int precision = GBC_PREC_F64;
+    int log_theta = 0;
+    bool mixed_dirty = true;
+    long long rowsq = 0, ldq = 0, Mpad = 0;
+    RawBuf q, qscale, x32, y32, st32, err;
+    alignas(128) unsigned char tmap[128];
     Integrator integ;
     std::vector<double> hstage;
 
@@ -145,7 +170,45 @@ struct gbc_model {
         for (int k = 0; k < 6; ++k) r.deps0[k] = deps0[k];
         r.xm = xm.p;
         r.skip = nullptr;
+        r.log_theta = 0;
+        r.mode = precision;
+        r.q = q.p;
+        r.qscale = static_cast<const float*>(qscale.p);
+        r.rowsq = rowsq; r.ldq = ldq; r.Mpad = Mpad;
+        r.tmap = tmap;
+        r.st32 = static_cast<const float*>(st32.p);
+        r.x32 = static_cast<float*>(x32.p);
+        r.y32 = static_cast<float*>(y32.p);
+        r.err = static_cast<int*>(err.p);
         return r;
+    }
+    // builds the block-scaled 16-bit copies when the mixed mode is on and the GFs changed
+    int prepare() {
+        if (precision == GBC_PREC_F64 || !mixed_dirty) return 0;
+        if (int rc = ready()) return rc;
+        Mpad = (M + 127) / 128 * 128;
+        rowsq = Mpad + (N + 127) / 128 * 128;
+        ldq = (npad + M + 255) / 256 * 256;
+        if (ne == 0) { rowsq = 128; ldq = 256; }
+        cudaStream_t s = stream;
+        if (int rc = st32.alloc(sizeof(float) * (size_t)nx * nxi * nxi)) return rc;
+        if (int rc = fault_f32(st.p, static_cast<float*>(st32.p), (long long)nx * nxi * nxi, s)) return rc;
+        if (int rc = y32.alloc(sizeof(float) * N)) return rc;
+        if (int rc = err.alloc(sizeof(int))) return rc;
+        GBC_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+        if (ne > 0) {
+            if (int rc = q.alloc(2 * (size_t)rowsq * ldq)) return rc;
+            if (int rc = qscale.alloc(sizeof(float) * (size_t)(rowsq / 128) * (ldq / 128))) return rc;
+            if (int rc = x32.alloc(sizeof(float) * (size_t)ldq)) return rc;
+            GBC_CUDA(cudaMemsetAsync(x32.p, 0, sizeof(float) * (size_t)ldq, s));
+            if (int rc = quantize_mantle(precision, N, npad, M, Mpad, rowsq, ldq, gm.p, ldm, g21.p, ld21, q.p,
+                                         static_cast<float*>(qscale.p), s))
+                return rc;
+            if (int rc = encode_qmap(precision, q.p, rowsq, ldq, tmap)) return rc;
+        }
+        GBC_CUDA(cudaStreamSynchronize(s));
+        mixed_dirty = false;
+        return 0;
     }
     int ready() const {
         if (!props) return fail(GBC_ESTATE, "fault properties not set (gbc_model_set_fault_props)");
@@ -426,6 +489,7 @@ int gbc_model_set_gf(gbc_model* m, int which, const double* host) {
         default:
             return fail(GBC_EINVAL, "unknown Green's function id");
     }
+    m->mixed_dirty = true;
     GBC_CUDA(cudaStreamSynchronize(s));
     return 0;
 }
@@ -495,23 +559,40 @@ int gbc_model_assemble(gbc_model* m, const gbc_fault_mesh* mf, const gbc_hex_mes
         g_launches += 3;
         m->has_g12 = m->has_g21 = m->has_g22 = true;
     }
+    m->mixed_dirty = true;
     GBC_CUDA(cudaStreamSynchronize(s));
     return 0;
 }
 
 int gbc_model_set_precision(gbc_model* m, int mode) {
     if (!m) return fail(GBC_EINVAL, "null model");
-    if (mode != GBC_PREC_F64) return fail(GBC_EINVAL, "precision mode not available in this build");
+    if (mode != GBC_PREC_F64 && mode != GBC_PREC_BF16 && mode != GBC_PREC_F16)
+        return fail(GBC_EINVAL, "unknown precision mode");
+    if (mode != m->precision) m->mixed_dirty = true;
     m->precision = mode;
     return 0;
+}
+
+int gbc_model_set_log_theta(gbc_model* m, int on) {
+    if (!m) return fail(GBC_EINVAL, "null model");
+    m->log_theta = on ? 1 : 0;
+    return 0;
+}
+
+int gbc_model_error_word(gbc_model* m) {
+    if (!m || !m->err.p) return 0;
+    int h = 0;
+    if (cudaMemcpy(&h, m->err.p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    return h;
 }
 
 int gbc_rhs_dev(gbc_model* m, double t, const double* u, double* du) {
     (void)t;
     if (!m || !u || !du) return fail(GBC_EINVAL, "null argument");
     if (int rc = m->ready()) return rc;
+    if (int rc = m->prepare()) return rc;
     if (int rc = launch_rhs(m->args(), u, du, m->stream)) return rc;
-    g_launches += (m->ne > 0) ? 2 : 1;
+    g_launches += rhs_kernel_count(m->args());
     return 0;
 }
 
@@ -520,6 +601,7 @@ int gbc_rhs(gbc_model* m, double t, const double* const* u_parts, double* const*
     const int want = m->ne > 0 ? 5 : 3;
     if (nparts != want) return fail(GBC_EINVAL, "ArrayPartition must have " + std::to_string(want) + " components");
     if (int rc = m->ready()) return rc;
+    if (int rc = m->prepare()) return rc;
     const long long N = m->N, E = m->M;
     long long len[5] = {N, N, N, 0, 0};
     if (want == 5) { len[2] = E; len[3] = E; len[4] = N; }
@@ -531,7 +613,7 @@ int gbc_rhs(gbc_model* m, double t, const double* const* u_parts, double* const*
         off += len[p];
     }
     if (int rc = launch_rhs(m->args(), m->u.p, m->du.p, s)) return rc;
-    g_launches += (m->ne > 0) ? 2 : 1;
+    g_launches += rhs_kernel_count(m->args());
     off = 0;
     for (int p = 0; p < want; ++p) {
         GBC_CUDA(cudaMemcpyAsync(du_parts[p], m->du.p + off, sizeof(double) * len[p], cudaMemcpyDeviceToHost, s));
@@ -541,19 +623,40 @@ int gbc_rhs(gbc_model* m, double t, const double* const* u_parts, double* const*
     return 0;
 }
 
+__global__ void k_theta_transform(double* th, int n, int to_log) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        th[i] = to_log ? log(th[i]) : exp(th[i]);
+}
+
+static int theta_transform(double* th, int n, int to_log, cudaStream_t s) {
+    k_theta_transform<<<(n + 255) / 256, 256, 0, s>>>(th, n, to_log);
+    GBC_CUDA(cudaGetLastError());
+    g_launches += 1;
+    return 0;
+}
+
 static int integrate_common(gbc_model* m, double* u_dev, double t0, double t1, const gbc_solver_opts* o,
                             gbc_solver_stats* st) {
     if (!o) return fail(GBC_EINVAL, "null solver options");
     if (!(o->reltol > 0) || !(o->abstol >= 0) || !(o->dt0 > 0) || !(o->dtmax > 0) || o->maxiters <= 0)
         return fail(GBC_EINVAL, "invalid solver options");
     if (int rc = m->ready()) return rc;
+    if (int rc = m->prepare()) return rc;
     if (int rc = integrator_alloc(m->integ, m->state_len())) return rc;
-    int rc = integrator_run(m->integ, m->args(), u_dev, t0, t1, o->reltol, o->abstol, o->dt0, o->dtmax,
+    RhsArgs args = m->args();
+    args.log_theta = m->log_theta;
+    if (m->log_theta) {
+        if (int rc = theta_transform(u_dev + m->N, m->N, 1, m->stream)) return rc;
+    }
+    int rc = integrator_run(m->integ, args, u_dev, t0, t1, o->reltol, o->abstol, o->dt0, o->dtmax,
                             o->dtmin, o->maxiters, m->stream);
+    if (m->log_theta) {
+        if (int rc2 = theta_transform(u_dev + m->N, m->N, 0, m->stream)) return rc2;
+    }
     const Ctrl& c = *m->integ.ctrl_host;
     // kernels enqueued: the FSAL seed RHS, then every kernel node of every graph launch (steps
     // past completion return at once but still count as launches)
-    const int rhs_k = (m->ne > 0) ? 2 : 1;
+    const int rhs_k = rhs_kernel_count(args);
     const long long per_step = 6LL * (1 + rhs_k) + 3;
     g_launches += rhs_k + m->integ.graph_launches * m->integ.steps_per_launch * per_step;
     if (st) {

@@ -26,6 +26,18 @@ struct RhsArgs {
     double* xm;
     // optional device flag: when non-null and nonzero the launch does nothing (finished solve)
     const int* skip;
+    // integrate ln θ instead of θ (the state's θ slot holds ψ = ln θ; dψ/dt = (1 - vθ/L)/θ)
+    int log_theta;
+    // ---- block-scaled 16-bit storage (GBC_PREC_BF16 / GBC_PREC_F16) --------------------------
+    int mode;                    // 0: FP64 path above; 1: BF16; 2: FP16
+    const void* q;               // (rowsq x ldq) 16-bit: rows [0,M) = [G12|0|G22], [Mpad,Mpad+N) = [0|G21]
+    const float* qscale;         // FP32 scale per 128x128 block, (rowsq/128) x (ldq/128)
+    long long rowsq, ldq, Mpad;
+    const void* tmap;            // host pointer to the CUtensorMap of q (box 256 x 32)
+    const float* st32;           // fault-fault Toeplitz kernel in FP32
+    float* x32;                  // [v - vpl; 0; dϵ - dϵ₀; 0] in FP32, length ldq
+    float* y32;                  // G21 part of the fault rows, length N
+    int* err;                    // device error word (bounded-wait timeouts)
 };
 
 // state offsets in the flat ArrayPartition layout
@@ -52,5 +64,17 @@ inline StateLayout layout_of(int N, int ne) {
 
 // Launches the RHS for the flat state u -> du on stream s (1 kernel fault-only, 2 viscoelastic).
 int launch_rhs(const RhsArgs& a, const double* u, double* du, cudaStream_t s);
+// Number of kernels one launch_rhs enqueues for these arguments.
+int rhs_kernel_count(const RhsArgs& a);
+
+// Block-scaled 16-bit path (mixed.cu)
+int launch_rhs_mixed(const RhsArgs& a, const double* u, double* du, cudaStream_t s);
+// Builds q and qscale from the FP64 rows (gm with ldm, g21 with ld21) on stream s.
+int quantize_mantle(int mode, int N, int npad, long long M, long long Mpad, long long rowsq, long long ldq,
+                    const double* gm, size_t ldm, const double* g21, size_t ld21, void* q, float* qscale,
+                    cudaStream_t s);
+// Encodes the TMA descriptor for q (rowsq x ldq 16-bit, box 256 columns x 32 rows).
+int encode_qmap(int mode, void* q, long long rowsq, long long ldq, void* tmap_out /* 128 B */);
+int fault_f32(const double* st, float* st32, long long n, cudaStream_t s);
 
 }  // namespace gbc

@@ -93,29 +93,38 @@ __global__ void __launch_bounds__(256) k_rows(RhsArgs a, const double* __restric
         // fault-fault traction rate: symmetric block-Toeplitz sum
         double acc = 0.0;
         const double* v = u + L.v;
-        for (int m = lane; m < N; m += 32) {
-            const int k = m % nx, l = m / nx;
-            const int d = ii > k ? ii - k : k - ii;
-            acc = fma(__ldg(a.st + d + (size_t)nx * (j + (size_t)nxi * l)), v[m] - a.vpl, acc);
+        for (int l = 0; l < nxi; ++l) {
+            const double* stl = a.st + (size_t)nx * (j + (size_t)nxi * l);
+            const double* vl = v + (size_t)nx * l;
+            for (int k = lane; k < nx; k += 32) {
+                const int d = ii > k ? ii - k : k - ii;
+                acc = fma(__ldg(stl + d), vl[k] - a.vpl, acc);
+            }
         }
         if (M > 0) acc += warp_dot(a.g21 + (size_t)i * a.ld21, a.xm + a.npad, M, lane);
         const double dtau = warp_sum(acc);
         if (lane == 0) {
-            const double vi = v[i], th = u[L.th + i];
+            const double vi = v[i], th = a.log_theta ? exp(u[L.th + i]) : u[L.th + i];
             const double ai = a.a[i], bi = a.b[i], Li = a.L[i];
             const double psi1 = exp((a.f0 + bi * log(a.v0 * fmax(0.0, th) / Li)) / ai) / (2.0 * a.v0);
             const double psi2 = a.sig[i] * psi1 / hypot(1.0, vi * psi1);
             const double dmu_dv = ai * psi2;
             const double dmu_dth = bi / th * vi * psi2;
             const double dth = 1.0 - vi * th / Li;
-            du[L.th + i] = dth;
+            du[L.th + i] = a.log_theta ? dth / th : dth;
             du[L.v + i] = (dtau - dmu_dth * dth) / (dmu_dv + a.eta);
             du[L.delta + i] = vi;
         }
     }
 }
 
+int rhs_kernel_count(const RhsArgs& a) {
+    if (a.mode != 0) return a.ne > 0 ? 3 : 1;
+    return a.ne > 0 ? 2 : 1;
+}
+
 int launch_rhs(const RhsArgs& a, const double* u, double* du, cudaStream_t s) {
+    if (a.mode != 0) return launch_rhs_mixed(a, u, du, s);
     const StateLayout L = layout_of(a.N, a.ne);
     const int sms = sm_count();
     if (a.ne > 0) {

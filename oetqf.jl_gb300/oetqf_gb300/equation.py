@@ -117,6 +117,12 @@ class GB300Model:
     def set_precision(self, mode: int):
         C.check(C.lib().gbc_model_set_precision(self.h, mode))
 
+    def set_log_theta(self, on: bool):
+        C.check(C.lib().gbc_model_set_log_theta(self.h, int(bool(on))))
+
+    def error_word(self) -> int:
+        return int(C.lib().gbc_model_error_word(self.h))
+
     # -- right-hand side --------------------------------------------------------------------------
     def rhs(self, du: ArrayPartition, u: ArrayPartition, t: float = 0.0):
         n = len(u.x)
