@@ -173,6 +173,39 @@ int gbc_rhs_visco_noalloc(int nx, int nxi, int ne, const double* st, const doubl
  * CUDA events around the library's launches. */
 void* gbc_model_stream(gbc_model* m);
 
+/* ---- Batched ensembles (many independent fault-only models in one persistent launch) -------- */
+
+typedef struct gbc_ensemble gbc_ensemble;
+
+/* nmodels fault-only models of sizes nx[i] x nxi[i] (each model's ODE is equation.jl:156-166).
+ * Each model runs on one CTA with its Toeplitz kernel in shared memory (FP32) and its own Tsit5
+ * step control; the state, friction and error norm are FP64. nx*nxi*nxi + nx*nxi floats of the
+ * largest model must fit in 200 KB. */
+int gbc_ensemble_create(int nmodels, const int* nx, const int* nxi, gbc_ensemble** out);
+void gbc_ensemble_destroy(gbc_ensemble* e);
+/* Per model, as for a single model: the reference's fourier or real fault-fault kernel
+ * (GBC_GF11_DFT / GBC_GF11_REAL, src/BEM/GF.jl:31-71), or assembled on the device. */
+int gbc_ensemble_set_gf(gbc_ensemble* e, int model, int which, const double* host);
+int gbc_ensemble_assemble(gbc_ensemble* e, int model, const gbc_fault_mesh* mf, double lambda,
+                          double mu, int ftype, int nrept, double buffer_ratio);
+int gbc_ensemble_set_fault_props(gbc_ensemble* e, int model, const double* a, const double* b,
+                                 const double* L, const double* sigma, double eta, double vpl,
+                                 double f0, double v0);
+/* Threads per model CTA (128, 256 or 512; picked by the autotuner in the host package). */
+int gbc_ensemble_set_block(gbc_ensemble* e, int threads);
+/* Integrate ψ = ln θ internally (default on; the caller's state keeps θ). */
+int gbc_ensemble_set_log_theta(gbc_ensemble* e, int on);
+/* The flat state is the concatenation over models of (v, θ, δ); model i starts at
+ * gbc_ensemble_state_offset(e, i). Each model integrates from t0[i] to t1[i]; stats has one entry
+ * per model. The _dev variant takes a device pointer. */
+long long gbc_ensemble_state_len(const gbc_ensemble* e);
+long long gbc_ensemble_state_offset(const gbc_ensemble* e, int model);
+int gbc_ensemble_integrate(gbc_ensemble* e, double* u, const double* t0, const double* t1,
+                           const gbc_solver_opts* opts, gbc_solver_stats* stats);
+int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0, const double* t1,
+                               const gbc_solver_opts* opts, gbc_solver_stats* stats);
+void* gbc_ensemble_stream(gbc_ensemble* e);
+
 /* ---- Diagnostics ------------------------------------------------------------------------ */
 int gbc_last_error(char* buf, size_t len);
 const char* gbc_version(void);

@@ -1,0 +1,542 @@
+// Batched ensemble: many independent fault-only cycle models of uneven size integrated in one
+// persistent launch, one CTA per model. Each CTA keeps its model's Toeplitz kernel (FP32) and the
+// slip-rate vector in shared memory and runs its own Tsit5 steps with its own dt (per-instance
+// step control); state, stage derivatives, the friction update and the error norm are FP64, the
+// traction-rate convolution accumulates in FP32. A launch runs at most `budget` steps per model
+// and returns; the host relaunches a captured CUDA graph of launches until every model is done.
+//
+// Reference: the fault-only ode (src/BEM/equation.jl:156-166) = relative_velocity! (:35-42),
+// dτ_dt! (:44-61, applied as the direct Toeplitz sum), update_fault! (:233-246) and the ageing
+// law (:279); the integrator stands in for OrdinaryDiffEq's solve (src/io.jl:125-130).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gbc_internal.cuh"
+
+namespace gbc {
+
+struct EnsModel {
+    int nx, nxi, N, log_theta;
+    long long off_n;   // patch offset (props); state offset is 3 * off_n
+    long long off_st;  // offset into st32
+    double eta, vpl, f0, v0;
+    double t, dt, t1, qold;
+    long long naccept, nreject, iters, maxiters;
+    int status, done, started, logged;  // logged: θ slot holds ln θ during this integration
+};
+
+struct EnsArgs {
+    EnsModel* models;
+    int nmodels;
+    const float* st32;
+    const double *a, *b, *L, *sig;
+    double* u;
+    double* k[7];
+    double* y;
+    double* un;
+    double reltol, abstol, dtmax, dtmin;
+    int budget;                      // step cap per launch and model
+    unsigned long long budget_ns;    // wall-clock budget per launch (all models stay busy until done)
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+__constant__ double e_ta[7][6] = {
+    {0},
+    {0.161},
+    {-0.008480655492356989, 0.335480655492357},
+    {2.897153057105493, -6.359448489975075, 4.3622954328695815},
+    {5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525},
+    {5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383},
+    {0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081, 2.324710524099774}};
+__constant__ double e_te[7] = {-0.00178001105222577714, -0.0008164344596567469, 0.007880878010261995,
+                               -0.1447110071732629, 0.5823571654525552, -0.45808210592918697,
+                               0.015151515151515152};
+
+// fault-only RHS of one model: y (v, θ-or-ψ, δ) -> k; st_s and rv_s are shared memory
+template <int BS>
+__device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, const float* st_s, float* rv_s,
+                                        const double* __restrict__ y, double* __restrict__ k) {
+    const int N = m.N, nx = m.nx, nxi = m.nxi;
+    const double* v = y;
+    const double* th = y + N;
+    for (int i = threadIdx.x; i < N; i += BS) rv_s[i] = (float)(v[i] - m.vpl);
+    __syncthreads();
+    const double* pa = A.a + m.off_n;
+    const double* pb = A.b + m.off_n;
+    const double* pL = A.L + m.off_n;
+    const double* ps = A.sig + m.off_n;
+    for (int i = threadIdx.x; i < N; i += BS) {
+        const int ii = i % nx, j = i / nx;
+        float acc = 0.f;
+        for (int l = 0; l < nxi; ++l) {
+            const float* stl = st_s + nx * (j + nxi * l);
+            const float* rl = rv_s + nx * l;
+#pragma unroll 4
+            for (int kk = 0; kk < nx; ++kk) {
+                const int d = ii > kk ? ii - kk : kk - ii;
+                acc = fmaf(stl[d], rl[kk], acc);
+            }
+        }
+        const double dtau = (double)acc;
+        const double vi = v[i];
+        const double tht = m.log_theta ? exp(th[i]) : th[i];
+        const double ai = pa[i], bi = pb[i], Li = pL[i];
+        const double psi1 = exp((m.f0 + bi * log(m.v0 * fmax(0.0, tht) / Li)) / ai) / (2.0 * m.v0);
+        const double psi2 = ps[i] * psi1 / hypot(1.0, vi * psi1);
+        const double dmu_dv = ai * psi2;
+        const double dmu_dth = bi / tht * vi * psi2;
+        const double dth = 1.0 - vi * tht / Li;
+        k[i] = (dtau - dmu_dth * dth) / (dmu_dv + m.eta);
+        k[N + i] = m.log_theta ? dth / tht : dth;
+        k[2 * N + i] = vi;
+    }
+    __syncthreads();
+}
+
+template <int BS>
+__global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
+    extern __shared__ __align__(16) float sm[];
+    __shared__ double red[BS / 32];
+    __shared__ int s_go, s_stop;
+    const unsigned long long t_launch = global_ns();
+    const int mi = blockIdx.x;
+    if (mi >= A.nmodels) return;
+    EnsModel& M = A.models[mi];
+    if (M.done) return;
+    const EnsModel m = M;  // sizes and constants (t, dt live in M)
+    const int N = m.N, n3 = 3 * N;
+    const int nst = m.nx * m.nxi * m.nxi;
+    float* st_s = sm;
+    float* rv_s = sm + nst;
+    for (int i = threadIdx.x; i < nst; i += BS) st_s[i] = A.st32[m.off_st + i];
+    __syncthreads();
+    const long long o3 = 3 * m.off_n;
+    double* u = A.u + o3;
+    double* kk[7];
+    for (int s = 0; s < 7; ++s) kk[s] = A.k[s] + o3;
+    double* y = A.y + o3;
+    double* un = A.un + o3;
+    if (!m.started) {  // FSAL seed
+        ens_rhs<BS>(m, A, st_s, rv_s, u, kk[0]);
+        if (threadIdx.x == 0) M.started = 1;
+    }
+    for (int step = 0; step < A.budget; ++step) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_stop = M.done || (global_ns() - t_launch > A.budget_ns);
+        __syncthreads();
+        if (s_stop) break;
+        const double dt = M.dt;
+        for (int s = 1; s < 7; ++s) {
+            double* dst = (s == 6) ? un : y;
+            for (int i = threadIdx.x; i < n3; i += BS) {
+                double acc = 0.0;
+                for (int r = 0; r < s; ++r) acc = fma(e_ta[s][r], kk[r][i], acc);
+                dst[i] = u[i] + dt * acc;
+            }
+            __syncthreads();
+            ens_rhs<BS>(m, A, st_s, rv_s, dst, kk[s]);
+        }
+        double ss = 0.0;
+        int bad = 0;
+        for (int i = threadIdx.x; i < n3; i += BS) {
+            double e = 0.0;
+#pragma unroll
+            for (int s = 0; s < 7; ++s) e = fma(e_te[s], kk[s][i], e);
+            e *= dt;
+            const double unv = un[i];
+            const double sc = A.abstol + A.reltol * fmax(fabs(u[i]), fabs(unv));
+            const double r = e / sc;
+            ss = fma(r, r, ss);
+            bad |= !isfinite(unv);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            ss += __shfl_xor_sync(0xffffffffu, ss, o);
+            bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+        }
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = bad ? INFINITY : ss;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tot = 0.0;
+            for (int w = 0; w < BS / 32; ++w) tot += red[w];
+            double EEst = sqrt(tot / (double)n3);
+            if (!isfinite(EEst)) EEst = INFINITY;
+            const double beta1 = 0.14, beta2 = 0.08, gam = 0.9, qmin = 0.2, qmax = 10.0;
+            const double q11 = pow(EEst, beta1);
+            M.iters += 1;
+            double dtn;
+            int acc = 0;
+            if (EEst <= 1.0) {
+                double q = q11 / pow(M.qold, beta2);
+                q = fmax(1.0 / qmax, fmin(1.0 / qmin, q / gam));
+                const double tn = M.t + dt;
+                M.t = (tn >= M.t1) ? M.t1 : tn;
+                M.qold = fmax(EEst, 1e-4);
+                M.naccept += 1;
+                acc = 1;
+                dtn = dt / q;
+            } else {
+                const double q = isfinite(q11) ? fmin(1.0 / qmin, q11 / gam) : 1.0 / qmin;
+                M.nreject += 1;
+                dtn = dt / q;
+            }
+            if (M.t >= M.t1) { M.done = 1; M.status = 0; }
+            else if (dtn < A.dtmin || !isfinite(dtn) || M.iters >= M.maxiters) { M.done = 1; M.status = -5; }
+            if (dtn > A.dtmax) dtn = A.dtmax;
+            const double rem = M.t1 - M.t;
+            if (dtn >= rem) dtn = rem;
+            M.dt = dtn;
+            s_go = acc;
+        }
+        __syncthreads();
+        if (s_go) {
+            for (int i = threadIdx.x; i < n3; i += BS) {
+                u[i] = un[i];
+                kk[0][i] = kk[6][i];
+            }
+        }
+    }
+}
+
+__global__ void k_ens_theta(EnsArgs A, int to_log) {
+    const EnsModel& m = A.models[blockIdx.x];
+    if (!m.logged) return;  // models with nothing to integrate keep θ untouched
+    double* th = A.u + 3 * m.off_n + m.N;
+    for (int i = threadIdx.x; i < m.N; i += blockDim.x) th[i] = to_log ? log(th[i]) : exp(th[i]);
+}
+
+}  // namespace gbc
+
+using namespace gbc;
+
+struct gbc_ensemble {
+    int n = 0;
+    std::vector<EnsModel> host;
+    std::vector<int> has_gf, has_props;
+    long long total_n = 0, total_st = 0;
+    int max_nst = 0, max_n = 0;
+    cudaStream_t stream = nullptr;
+    EnsModel* d_models = nullptr;
+    float* st32 = nullptr;
+    double *a = nullptr, *b = nullptr, *L = nullptr, *sig = nullptr, *u = nullptr, *y = nullptr, *un = nullptr;
+    double* k[7] = {};
+    int block = 256;
+    int log_theta = 1;
+    cudaGraphExec_t exec = nullptr;
+    int exec_block = 0, exec_budget = 0;
+};
+
+namespace gbc {
+void count_launches(long long n);
+int launch_gf_ff(const FaultDev& f, double lambda, double mu, int ftype, int nrept, double buffer_ratio, double* st,
+                 cudaStream_t s);
+}
+
+static int ens_free(gbc_ensemble* e) {
+    if (e->exec) cudaGraphExecDestroy(e->exec);
+    void* ptrs[] = {e->d_models, e->st32, e->a, e->b, e->L, e->sig, e->u, e->y, e->un};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    for (int s = 0; s < 7; ++s)
+        if (e->k[s]) cudaFree(e->k[s]);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    return 0;
+}
+
+__global__ void k_f64_to_f32(const double* __restrict__ a, float* __restrict__ b, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+namespace gbc {
+int launch_gf_ff_idft(int nx, int nxi, const double* st_dft, double* st, cudaStream_t s);
+}
+
+extern "C" {
+
+int gbc_ensemble_create(int nmodels, const int* nx, const int* nxi, gbc_ensemble** out) {
+    if (!out) return fail(GBC_EINVAL, "null output handle");
+    *out = nullptr;
+    if (nmodels <= 0 || !nx || !nxi) return fail(GBC_EINVAL, "ensemble needs at least one model");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(GBC_ENODEV, "no CUDA device available (libgbcycle has no CPU fallback)");
+    gbc_ensemble* e = new gbc_ensemble();
+    e->n = nmodels;
+    e->host.resize(nmodels);
+    e->has_gf.assign(nmodels, 0);
+    e->has_props.assign(nmodels, 0);
+    long long on = 0, os = 0;
+    for (int i = 0; i < nmodels; ++i) {
+        if (nx[i] <= 0 || nxi[i] <= 0) { delete e; return fail(GBC_EINVAL, "model sizes must be positive"); }
+        EnsModel& m = e->host[i];
+        memset(&m, 0, sizeof(m));
+        m.nx = nx[i]; m.nxi = nxi[i]; m.N = nx[i] * nxi[i];
+        m.off_n = on; m.off_st = os;
+        on += m.N;
+        os += (long long)nx[i] * nxi[i] * nxi[i];
+        e->max_nst = std::max(e->max_nst, nx[i] * nxi[i] * nxi[i]);
+        e->max_n = std::max(e->max_n, m.N);
+    }
+    e->total_n = on;
+    e->total_st = os;
+    const size_t smem = sizeof(float) * ((size_t)e->max_nst + e->max_n);
+    if (smem > 200 * 1024) { delete e; return fail(GBC_EINVAL, "largest ensemble model exceeds the shared-memory budget (nx*nxi*nxi + nx*nxi floats <= 200 KB)"); }
+    int rc = 0;
+    cudaError_t ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) rc = cuda_fail(ce, "cudaStreamCreate");
+    auto A = [&](void** p, size_t bytes) {
+        if (rc) return;
+        cudaError_t c2 = cudaMalloc(p, bytes);
+        if (c2 != cudaSuccess) rc = cuda_fail(c2, "cudaMalloc");
+    };
+    A((void**)&e->d_models, sizeof(EnsModel) * nmodels);
+    A((void**)&e->st32, sizeof(float) * os);
+    for (double** p : {&e->a, &e->b, &e->L, &e->sig}) A((void**)p, sizeof(double) * on);
+    for (double** p : {&e->u, &e->y, &e->un}) A((void**)p, sizeof(double) * 3 * on);
+    for (int s = 0; s < 7; ++s) A((void**)&e->k[s], sizeof(double) * 3 * on);
+    if (rc) { ens_free(e); delete e; return rc; }
+    *out = e;
+    return 0;
+}
+
+void gbc_ensemble_destroy(gbc_ensemble* e) {
+    if (!e) return;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    ens_free(e);
+    delete e;
+}
+
+long long gbc_ensemble_state_offset(const gbc_ensemble* e, int model) {
+    if (!e || model < 0 || model >= e->n) return -1;
+    return 3 * e->host[model].off_n;
+}
+
+long long gbc_ensemble_state_len(const gbc_ensemble* e) { return e ? 3 * e->total_n : 0; }
+
+int gbc_ensemble_set_gf(gbc_ensemble* e, int model, int which, const double* host) {
+    if (!e || !host || model < 0 || model >= e->n) return fail(GBC_EINVAL, "bad ensemble model or buffer");
+    const EnsModel& m = e->host[model];
+    const size_t nst = (size_t)m.nx * m.nxi * m.nxi;
+    double *d1 = nullptr, *d2 = nullptr;
+    GBC_CUDA(cudaMalloc(&d1, sizeof(double) * nst * (which == GBC_GF11_DFT ? 3 : 1)));
+    int rc = 0;
+    if (which == GBC_GF11_DFT) {
+        d2 = d1 + 2 * nst;
+        cudaError_t c = cudaMemcpyAsync(d1, host, sizeof(double) * 2 * nst, cudaMemcpyHostToDevice, e->stream);
+        if (c != cudaSuccess) rc = cuda_fail(c, "cudaMemcpyAsync");
+        if (!rc) rc = launch_gf_ff_idft(m.nx, m.nxi, d1, d2, e->stream);
+        count_launches(1);
+    } else if (which == GBC_GF11_REAL) {
+        d2 = d1;
+        cudaError_t c = cudaMemcpyAsync(d1, host, sizeof(double) * nst, cudaMemcpyHostToDevice, e->stream);
+        if (c != cudaSuccess) rc = cuda_fail(c, "cudaMemcpyAsync");
+    } else {
+        rc = fail(GBC_EINVAL, "ensembles hold fault-only models (GBC_GF11_REAL or GBC_GF11_DFT)");
+    }
+    if (!rc) {
+        k_f64_to_f32<<<64, 256, 0, e->stream>>>(d2, e->st32 + m.off_st, (long long)nst);
+        count_launches(1);
+        cudaError_t c = cudaStreamSynchronize(e->stream);
+        if (c != cudaSuccess) rc = cuda_fail(c, "cudaStreamSynchronize");
+    }
+    cudaFree(d1);
+    if (!rc) e->has_gf[model] = 1;
+    return rc;
+}
+
+int gbc_ensemble_assemble(gbc_ensemble* e, int model, const gbc_fault_mesh* mf, double lambda, double mu, int ftype,
+                          int nrept, double buffer_ratio) {
+    if (!e || model < 0 || model >= e->n || !mf) return fail(GBC_EINVAL, "bad ensemble model or mesh");
+    const EnsModel& m = e->host[model];
+    if (mf->nx != m.nx || mf->nxi != m.nxi) return fail(GBC_EINVAL, "fault mesh does not match the model");
+    if (!(buffer_ratio >= 0)) return fail(GBC_EINVAL, "Argument `buffer_ratio` must be ≥ 0.");
+    std::vector<double> ax(mf->ax, mf->ax + 2 * mf->nx), axi(mf->axi, mf->axi + 2 * mf->nxi);
+    const size_t nst = (size_t)m.nx * m.nxi * m.nxi;
+    double* d = nullptr;
+    size_t need = nst + 3 * (size_t)mf->nxi + mf->nx + 2 * (size_t)mf->nx + 2 * (size_t)mf->nxi;
+    GBC_CUDA(cudaMalloc(&d, sizeof(double) * need));
+    double* st = d;
+    double* dx = st + nst;
+    double* dy = dx + mf->nx;
+    double* dz = dy + mf->nxi;
+    double* dax = dz + mf->nxi;
+    double* daxi = dax + 2 * mf->nx;
+    int rc = 0;
+    auto up = [&](double* dst, const double* src, size_t n) {
+        if (rc) return;
+        cudaError_t c = cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, e->stream);
+        if (c != cudaSuccess) rc = cuda_fail(c, "cudaMemcpyAsync");
+    };
+    up(dx, mf->x, mf->nx);
+    up(dy, mf->y, mf->nxi);
+    up(dz, mf->z, mf->nxi);
+    up(dax, mf->ax, 2 * mf->nx);
+    up(daxi, mf->axi, 2 * mf->nxi);
+    if (!rc) {
+        FaultDev f{mf->nx, mf->nxi, dx, dy, dz, dax, daxi, mf->dx, mf->dep, mf->dip};
+        rc = launch_gf_ff(f, lambda, mu, ftype, nrept, buffer_ratio, st, e->stream);
+    }
+    if (!rc) {
+        k_f64_to_f32<<<64, 256, 0, e->stream>>>(st, e->st32 + m.off_st, (long long)nst);
+        count_launches(2);
+        cudaError_t c = cudaStreamSynchronize(e->stream);
+        if (c != cudaSuccess) rc = cuda_fail(c, "cudaStreamSynchronize");
+    }
+    cudaFree(d);
+    if (!rc) e->has_gf[model] = 1;
+    return rc;
+}
+
+int gbc_ensemble_set_fault_props(gbc_ensemble* e, int model, const double* a, const double* b, const double* L,
+                                 const double* sigma, double eta, double vpl, double f0, double v0) {
+    if (!e || model < 0 || model >= e->n || !a || !b || !L || !sigma) return fail(GBC_EINVAL, "bad argument");
+    if (!(f0 > 0) || !(v0 > 0) || !(eta > 0) || !(vpl > 0)) return fail(GBC_EINVAL, "AssertionError: f₀, v₀, η, vpl must be > 0");
+    EnsModel& m = e->host[model];
+    const size_t N = m.N;
+    GBC_CUDA(cudaMemcpyAsync(e->a + m.off_n, a, sizeof(double) * N, cudaMemcpyHostToDevice, e->stream));
+    GBC_CUDA(cudaMemcpyAsync(e->b + m.off_n, b, sizeof(double) * N, cudaMemcpyHostToDevice, e->stream));
+    GBC_CUDA(cudaMemcpyAsync(e->L + m.off_n, L, sizeof(double) * N, cudaMemcpyHostToDevice, e->stream));
+    GBC_CUDA(cudaMemcpyAsync(e->sig + m.off_n, sigma, sizeof(double) * N, cudaMemcpyHostToDevice, e->stream));
+    GBC_CUDA(cudaStreamSynchronize(e->stream));
+    m.eta = eta; m.vpl = vpl; m.f0 = f0; m.v0 = v0;
+    e->has_props[model] = 1;
+    return 0;
+}
+
+int gbc_ensemble_set_block(gbc_ensemble* e, int threads) {
+    if (!e || (threads != 128 && threads != 256 && threads != 512)) return fail(GBC_EINVAL, "block must be 128, 256 or 512");
+    e->block = threads;
+    return 0;
+}
+
+int gbc_ensemble_set_log_theta(gbc_ensemble* e, int on) {
+    if (!e) return fail(GBC_EINVAL, "null ensemble");
+    e->log_theta = on ? 1 : 0;
+    return 0;
+}
+
+static int ens_launch(gbc_ensemble* e, const EnsArgs& A, int block, cudaStream_t s) {
+    const size_t smem = sizeof(float) * ((size_t)e->max_nst + e->max_n);
+    switch (block) {
+        case 128:
+            GBC_CUDA(cudaFuncSetAttribute(k_ensemble<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_ensemble<128><<<e->n, 128, smem, s>>>(A);
+            break;
+        case 512:
+            GBC_CUDA(cudaFuncSetAttribute(k_ensemble<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_ensemble<512><<<e->n, 512, smem, s>>>(A);
+            break;
+        default:
+            GBC_CUDA(cudaFuncSetAttribute(k_ensemble<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_ensemble<256><<<e->n, 256, smem, s>>>(A);
+    }
+    GBC_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// Integrates every model (or only those with active != 0 when given) from its current state to its
+// own t1; state u is the concatenation of the models' (v, θ, δ) on the device.
+int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0, const double* t1,
+                               const gbc_solver_opts* o, gbc_solver_stats* stats) {
+    if (!e || !u_dev || !t0 || !t1 || !o) return fail(GBC_EINVAL, "null argument");
+    if (!(o->reltol > 0) || !(o->abstol >= 0) || !(o->dt0 > 0) || !(o->dtmax > 0) || o->maxiters <= 0)
+        return fail(GBC_EINVAL, "invalid solver options");
+    for (int i = 0; i < e->n; ++i)
+        if (!e->has_gf[i] || !e->has_props[i]) return fail(GBC_ESTATE, "ensemble model " + std::to_string(i) + " is missing its Green's function or properties");
+    for (int i = 0; i < e->n; ++i) {
+        EnsModel& m = e->host[i];
+        m.t = t0[i]; m.t1 = t1[i];
+        m.dt = std::min(o->dt0, o->dtmax);
+        if (m.dt > t1[i] - t0[i]) m.dt = t1[i] - t0[i];
+        m.qold = 1e-4;
+        m.naccept = m.nreject = m.iters = 0;
+        m.maxiters = o->maxiters;
+        m.status = 0;
+        m.done = (t1[i] <= t0[i]) ? 1 : 0;
+        m.started = 0;
+        m.log_theta = e->log_theta && !m.done;
+        m.logged = m.log_theta;
+    }
+    cudaStream_t s = e->stream;
+    GBC_CUDA(cudaMemcpyAsync(e->d_models, e->host.data(), sizeof(EnsModel) * e->n, cudaMemcpyHostToDevice, s));
+    if (u_dev != e->u) GBC_CUDA(cudaMemcpyAsync(e->u, u_dev, sizeof(double) * 3 * e->total_n, cudaMemcpyDeviceToDevice, s));
+    EnsArgs A{};
+    A.models = e->d_models; A.nmodels = e->n; A.st32 = e->st32;
+    A.a = e->a; A.b = e->b; A.L = e->L; A.sig = e->sig;
+    A.u = e->u; for (int k = 0; k < 7; ++k) A.k[k] = e->k[k];
+    A.y = e->y; A.un = e->un;
+    A.reltol = o->reltol; A.abstol = o->abstol; A.dtmax = o->dtmax; A.dtmin = o->dtmin;
+    A.budget = 1 << 20;
+    A.budget_ns = 250000000ull;  // 250 ms per launch
+    if (e->log_theta) {
+        k_ens_theta<<<e->n, 256, 0, s>>>(A, 1);
+        GBC_CUDA(cudaGetLastError());
+        count_launches(1);
+    }
+    // a captured group of persistent launches, relaunched until every model reports done
+    const int group = 4;
+    if (!e->exec || e->exec_block != e->block) {
+        if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
+        cudaGraph_t g;
+        GBC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int rc = 0;
+        for (int k = 0; k < group && !rc; ++k) rc = ens_launch(e, A, e->block, s);
+        cudaError_t ce = cudaStreamEndCapture(s, &g);
+        if (rc) return rc;
+        GBC_CUDA(ce);
+        GBC_CUDA(cudaGraphInstantiate(&e->exec, g, 0));
+        cudaGraphDestroy(g);
+        e->exec_block = e->block;
+    }
+    for (;;) {
+        GBC_CUDA(cudaGraphLaunch(e->exec, s));
+        count_launches(group);
+        GBC_CUDA(cudaMemcpyAsync(e->host.data(), e->d_models, sizeof(EnsModel) * e->n, cudaMemcpyDeviceToHost, s));
+        GBC_CUDA(cudaStreamSynchronize(s));
+        bool all = true;
+        for (int i = 0; i < e->n; ++i) all &= (e->host[i].done != 0);
+        if (all) break;
+    }
+    if (e->log_theta) {
+        k_ens_theta<<<e->n, 256, 0, s>>>(A, 0);
+        GBC_CUDA(cudaGetLastError());
+        count_launches(1);
+    }
+    if (u_dev != e->u) GBC_CUDA(cudaMemcpyAsync(u_dev, e->u, sizeof(double) * 3 * e->total_n, cudaMemcpyDeviceToDevice, s));
+    GBC_CUDA(cudaStreamSynchronize(s));
+    int status = 0;
+    for (int i = 0; i < e->n; ++i) {
+        const EnsModel& m = e->host[i];
+        if (stats) {
+            stats[i].naccept = m.naccept; stats[i].nreject = m.nreject; stats[i].nrhs = 6 * m.iters + 1;
+            stats[i].t = m.t; stats[i].dt = m.dt; stats[i].status = m.status;
+        }
+        if (m.status != 0) status = GBC_ESOLVER;
+    }
+    if (status) return fail(GBC_ESOLVER, "at least one ensemble model stopped early");
+    return 0;
+}
+
+int gbc_ensemble_integrate(gbc_ensemble* e, double* u_host, const double* t0, const double* t1,
+                           const gbc_solver_opts* o, gbc_solver_stats* stats) {
+    if (!e || !u_host) return fail(GBC_EINVAL, "null argument");
+    GBC_CUDA(cudaMemcpyAsync(e->u, u_host, sizeof(double) * 3 * e->total_n, cudaMemcpyHostToDevice, e->stream));
+    int rc = gbc_ensemble_integrate_dev(e, e->u, t0, t1, o, stats);
+    if (rc != 0 && rc != GBC_ESOLVER) return rc;
+    GBC_CUDA(cudaMemcpyAsync(u_host, e->u, sizeof(double) * 3 * e->total_n, cudaMemcpyDeviceToHost, e->stream));
+    GBC_CUDA(cudaStreamSynchronize(e->stream));
+    return rc;
+}
+
+void* gbc_ensemble_stream(gbc_ensemble* e) { return e ? (void*)e->stream : nullptr; }
+
+}  // extern "C"

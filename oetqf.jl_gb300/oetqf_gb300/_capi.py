@@ -72,6 +72,14 @@ def lib():
             "gbc_last_error": [ctypes.c_char_p, ctypes.c_size_t],
             "gbc_model_set_log_theta": [P, I],
             "gbc_model_error_word": [P],
+            "gbc_ensemble_create": [I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(P)],
+            "gbc_ensemble_set_gf": [P, I, I, PD],
+            "gbc_ensemble_assemble": [P, I, ctypes.POINTER(FaultMesh), D, D, I, I, D],
+            "gbc_ensemble_set_fault_props": [P, I, PD, PD, PD, PD, D, D, D, D],
+            "gbc_ensemble_set_block": [P, I],
+            "gbc_ensemble_set_log_theta": [P, I],
+            "gbc_ensemble_integrate": [P, PD, PD, PD, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
+            "gbc_ensemble_integrate_dev": [P, P, PD, PD, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -85,6 +93,14 @@ def lib():
         L.gbc_rhs_visco_noalloc.argtypes = [I, I, I, P, P, ctypes.c_size_t, P, ctypes.c_size_t, P, P, P, P, D, D, D, D,
                                             P, P, PD, P, P, P]
         L.gbc_rhs_visco_noalloc.restype = I
+        L.gbc_ensemble_destroy.argtypes = [P]
+        L.gbc_ensemble_destroy.restype = None
+        L.gbc_ensemble_state_len.argtypes = [P]
+        L.gbc_ensemble_state_len.restype = LL
+        L.gbc_ensemble_state_offset.argtypes = [P, I]
+        L.gbc_ensemble_state_offset.restype = LL
+        L.gbc_ensemble_stream.argtypes = [P]
+        L.gbc_ensemble_stream.restype = P
         L.gbc_model_stream.argtypes = [P]
         L.gbc_model_stream.restype = P
         L.gbc_version.restype = ctypes.c_char_p

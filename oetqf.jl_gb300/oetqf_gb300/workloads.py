@@ -6,6 +6,11 @@ Random draws come from one splitmix64 stream (seeded) so CPU and GPU see identic
     Vpl = 1e-9 m/s, initial v = Vpl and θ = Dc/Vpl (1 + 0.01 U(-1,1)).
   * strike_slip_with_mantle(): the same friction over a Maxwell mantle (η_v = 1e19 Pa s, so
     γ = 1/(2η_v), n = 0) spanning 10-30 km depth, with lognormal Dc (median 12 mm, σ_ln 0.3).
+  * large_fault_with_mantle(): 256 x 16 patches at 0.5 km (4096) over 40 x 20 x 10 = 8000 cells
+    (x over the fault length, y over 40 km centred, 10-30 km depth), same friction, 200 years.
+  * fault_ensemble(): independent fault-only models with N ~ U[200, 2000] patches (10 rows of
+    1 km cells, nx = round(N/10)); per model a - b ~ U(-0.006, 0.004) on the 2-8 km zone (a = 0.015
+    there, 0.025 / b = 0.019 elsewhere), Dc lognormal (median 10 mm, σ_ln 0.3), σ ~ U(30, 80) MPa.
 """
 from __future__ import annotations
 
@@ -98,3 +103,30 @@ def strike_slip_with_mantle(length=100e3, depth=10e3, cell=1e3, mantle_cells=(50
     th0 = pf.L.reshape(-1, order="F") / VPL * (1 + 0.01 * (2 * rng.uniform(N) - 1))
     u0 = np.concatenate([np.full(N, VPL), th0, np.zeros(E), np.zeros(E), np.zeros(N)])
     return CycleModel(mf, ma, pf, pa, u0, years * YEAR, name=f"fault {mf.nx}x{mf.nξ} + mantle {ma.ne}")
+
+
+def large_fault_with_mantle(years=200.0, seed=1) -> CycleModel:
+    return strike_slip_with_mantle(length=128e3, depth=8e3, cell=0.5e3, mantle_cells=(40, 20, 10), mantle_y=40e3,
+                                   mantle_top=-10e3, mantle_bottom=-30e3, years=years, seed=seed)
+
+
+def fault_ensemble(n_models=256, years=50.0, seed=3, n_range=(200, 2000), nxi=10) -> list[CycleModel]:
+    rng = SplitMix64(seed)
+    out = []
+    for m in range(n_models):
+        N = n_range[0] + (n_range[1] - n_range[0]) * rng.uniform(1)[0]
+        nx = max(2, int(round(N / nxi)))
+        mf = gen_mesh("RectOkada", nx * 1e3, nxi * 1e3, 1e3, 1e3, 90.0)
+        amb = -0.006 + 0.010 * rng.uniform(1)[0]
+        sigma = 30e6 + 50e6 * rng.uniform(1)[0]
+        depth = -np.tile(mf.z, (mf.nx, 1))
+        vw = (depth >= 2e3) & (depth <= 8e3)
+        a = np.where(vw, 0.015, 0.025)
+        b = np.where(vw, 0.015 - amb, 0.019)
+        L = 0.010 * np.exp(0.3 * rng.normal(mf.nx * mf.nξ)).reshape((mf.nx, mf.nξ), order="F")
+        pf = RateStateQuasiDynamicProperty(a, b, L, np.full_like(a, sigma), MU / (2 * VS), VPL, 0.6, 1e-6)
+        Nn = mf.nx * mf.nξ
+        th0 = pf.L.reshape(-1, order="F") / VPL * (1 + 0.01 * (2 * rng.uniform(Nn) - 1))
+        u0 = np.concatenate([np.full(Nn, VPL), th0, np.zeros(Nn)])
+        out.append(CycleModel(mf, None, pf, None, u0, years * YEAR, name=f"ensemble member {m} ({mf.nx}x{mf.nξ})"))
+    return out
