@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -21,8 +22,9 @@ namespace gbc {
 
 struct EnsModel {
     int nx, nxi, N, log_theta;
+    int P, logP;       // FFT length (power of two >= 2nx - 1) and its log2
     long long off_n;   // patch offset (props); state offset is 3 * off_n
-    long long off_st;  // offset into st32
+    long long off_st;  // offset into the real spectra ghat: (nxi, nxi, P/2 + 1) floats
     double eta, vpl, f0, v0;
     double t, dt, t1, qold;
     long long naccept, nreject, iters, maxiters;
@@ -32,8 +34,9 @@ struct EnsModel {
 struct EnsArgs {
     EnsModel* models;
     int nmodels;
-    const float* st32;
+    const float* ghat;           // real spectra of the symmetric circulant kernels
     const double *a, *b, *L, *sig;
+    const double* c1;            // f0/a + (b/a) ln(v0/L) - ln(2 v0): ln ψ1 = c1 + (b/a) ln θ
     double* u;
     double* k[7];
     double* y;
@@ -61,42 +64,123 @@ __constant__ double e_te[7] = {-0.00178001105222577714, -0.0008164344596567469, 
                                -0.1447110071732629, 0.5823571654525552, -0.45808210592918697,
                                0.015151515151515152};
 
-// fault-only RHS of one model: y (v, θ-or-ψ, δ) -> k; st_s and rv_s are shared memory
+// Shared-memory layout of one model CTA (floats): complex FFT work arrays Z (nq x P), real-input
+// spectra X (nxi x H complex), twiddles (P/2 complex).
+struct EnsSmem {
+    float2* Z;
+    float2* X;
+    float2* tw;
+};
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+
+// in-place radix-2 DIT FFT of nq arrays of length P already in bit-reversed order; sign -1
+// forward (twiddles e^{-2πi t/P}), +1 inverse (conjugated twiddles, no scaling)
 template <int BS>
-__device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, const float* st_s, float* rv_s,
+__device__ __forceinline__ void fft_many(float2* Z, int nq, int P, int logP, const float2* tw, int inverse) {
+    const int half_total = P >> 1;
+    for (int st = 0; st < logP; ++st) {
+        const int half = 1 << st;
+        const int tstride = P >> (st + 1);
+        for (int t = threadIdx.x; t < nq * half_total; t += BS) {
+            const int q = t / half_total, b = t - q * half_total;
+            const int grp = b >> st, pos = b & (half - 1);
+            const int i0 = (grp << (st + 1)) + pos, i1 = i0 + half;
+            float2 w = tw[pos * tstride];
+            if (inverse) w.y = -w.y;
+            float2* z = Z + q * P;
+            const float2 a = z[i0], c = cmul(z[i1], w);
+            z[i0] = make_float2(a.x + c.x, a.y + c.y);
+            z[i1] = make_float2(a.x - c.x, a.y - c.y);
+        }
+        __syncthreads();
+    }
+}
+
+// fault-only RHS of one model: y (v, θ-or-ψ, δ) -> k. The traction rate is the rFFT convolution
+// of the reference (equation.jl:44-61) done in shared memory: two real rows per complex FFT,
+// a real per-frequency mixing (the symmetric circulant kernel has a real spectrum), two output
+// rows per inverse FFT.
+template <int BS>
+__device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, const EnsSmem& S,
                                         const double* __restrict__ y, double* __restrict__ k) {
-    const int N = m.N, nx = m.nx, nxi = m.nxi;
+    const int N = m.N, nx = m.nx, nxi = m.nxi, P = m.P, logP = m.logP, H = P / 2 + 1;
+    const int nq = (nxi + 1) / 2;
     const double* v = y;
     const double* th = y + N;
-    for (int i = threadIdx.x; i < N; i += BS) rv_s[i] = (float)(v[i] - m.vpl);
+    // pack rows (2q, 2q+1) as real/imag, zero padded, in bit-reversed order
+    for (int t = threadIdx.x; t < nq * P; t += BS) {
+        const int q = t / P, i = t - q * P;
+        float re = 0.f, im = 0.f;
+        if (i < nx) {
+            re = (float)(v[i + nx * (2 * q)] - m.vpl);
+            if (2 * q + 1 < nxi) im = (float)(v[i + nx * (2 * q + 1)] - m.vpl);
+        }
+        S.Z[q * P + (__brev(i) >> (32 - logP))] = make_float2(re, im);
+    }
     __syncthreads();
+    fft_many<BS>(S.Z, nq, P, logP, S.tw, 0);
+    // separate the two real spectra: X_{2q}[f] = (Z[f] + conj Z[P-f]) / 2, X_{2q+1} = (Z[f] - conj Z[P-f]) / 2i
+    for (int t = threadIdx.x; t < nq * H; t += BS) {
+        const int q = t / H, f = t - q * H;
+        const float2 a = S.Z[q * P + f], b = S.Z[q * P + ((P - f) & (P - 1))];
+        S.X[(2 * q) * H + f] = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+        if (2 * q + 1 < nxi) S.X[(2 * q + 1) * H + f] = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
+    }
+    __syncthreads();
+    // Y_j[f] = sum_l G[j,l,f] X_l[f] (G real); repack (2q, 2q+1) as Y_2q + i Y_2q+1 with Hermitian fill,
+    // bit-reversed for the inverse transform
+    const float* G = A.ghat + m.off_st;
+    for (int t = threadIdx.x; t < nq * H; t += BS) {
+        const int q = t / H, f = t - q * H;
+        const int j0 = 2 * q, j1 = 2 * q + 1;
+        float2 y0 = make_float2(0.f, 0.f), y1 = make_float2(0.f, 0.f);
+        for (int l = 0; l < nxi; ++l) {
+            const float2 x = S.X[l * H + f];
+            const float g0 = __ldg(G + ((size_t)(j0 * nxi + l)) * H + f);
+            y0.x = fmaf(g0, x.x, y0.x);
+            y0.y = fmaf(g0, x.y, y0.y);
+            if (j1 < nxi) {
+                const float g1 = __ldg(G + ((size_t)(j1 * nxi + l)) * H + f);
+                y1.x = fmaf(g1, x.x, y1.x);
+                y1.y = fmaf(g1, x.y, y1.y);
+            }
+        }
+        // W[f] = Y0[f] + i Y1[f]; W[P-f] = conj(Y0[f]) + i conj(Y1[f])
+        float2* W = S.Z + q * P;
+        W[__brev(f) >> (32 - logP)] = make_float2(y0.x - y1.y, y0.y + y1.x);
+        if (f > 0 && f < P - f) W[__brev(P - f) >> (32 - logP)] = make_float2(y0.x + y1.y, -y0.y + y1.x);
+    }
+    __syncthreads();
+    fft_many<BS>(S.Z, nq, P, logP, S.tw, 1);
+    const double invP = 1.0 / P;
     const double* pa = A.a + m.off_n;
     const double* pb = A.b + m.off_n;
     const double* pL = A.L + m.off_n;
     const double* ps = A.sig + m.off_n;
+    const double* pc = A.c1 + m.off_n;
     for (int i = threadIdx.x; i < N; i += BS) {
         const int ii = i % nx, j = i / nx;
-        float acc = 0.f;
-        for (int l = 0; l < nxi; ++l) {
-            const float* stl = st_s + nx * (j + nxi * l);
-            const float* rl = rv_s + nx * l;
-#pragma unroll 4
-            for (int kk = 0; kk < nx; ++kk) {
-                const int d = ii > kk ? ii - kk : kk - ii;
-                acc = fmaf(stl[d], rl[kk], acc);
-            }
-        }
-        const double dtau = (double)acc;
+        const float2 w = S.Z[(j >> 1) * P + ii];
+        const double dtau = (double)((j & 1) ? w.y : w.x) * invP;
         const double vi = v[i];
-        const double tht = m.log_theta ? exp(th[i]) : th[i];
         const double ai = pa[i], bi = pb[i], Li = pL[i];
-        const double psi1 = exp((m.f0 + bi * log(m.v0 * fmax(0.0, tht) / Li)) / ai) / (2.0 * m.v0);
-        const double psi2 = ps[i] * psi1 / hypot(1.0, vi * psi1);
-        const double dmu_dv = ai * psi2;
-        const double dmu_dth = bi / tht * vi * psi2;
-        const double dth = 1.0 - vi * tht / Li;
-        k[i] = (dtau - dmu_dth * dth) / (dmu_dv + m.eta);
-        k[N + i] = m.log_theta ? dth / tht : dth;
+        if (m.log_theta) {
+            // ψ = ln θ: ψ1 = exp(c1 + (b/a) ψ), 1/θ = exp(-ψ); dψ = 1/θ - v/L; dμ/dθ dθ = b v ψ2 dψ
+            const double psi = th[i];
+            const double psi1 = exp(pc[i] + (bi / ai) * psi);
+            const double psi2 = ps[i] * psi1 / sqrt(fma(vi * psi1, vi * psi1, 1.0));
+            const double dpsi = exp(-psi) - vi / Li;
+            k[i] = (dtau - bi * vi * psi2 * dpsi) / (ai * psi2 + m.eta);
+            k[N + i] = dpsi;
+        } else {
+            const double tht = th[i];
+            const double psi1 = exp((m.f0 + bi * log(m.v0 * fmax(0.0, tht) / Li)) / ai) / (2.0 * m.v0);
+            const double psi2 = ps[i] * psi1 / hypot(1.0, vi * psi1);
+            const double dth = 1.0 - vi * tht / Li;
+            k[i] = (dtau - bi / tht * vi * psi2 * dth) / (ai * psi2 + m.eta);
+            k[N + i] = dth;
+        }
         k[2 * N + i] = vi;
     }
     __syncthreads();
@@ -114,10 +198,16 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
     if (M.done) return;
     const EnsModel m = M;  // sizes and constants (t, dt live in M)
     const int N = m.N, n3 = 3 * N;
-    const int nst = m.nx * m.nxi * m.nxi;
-    float* st_s = sm;
-    float* rv_s = sm + nst;
-    for (int i = threadIdx.x; i < nst; i += BS) st_s[i] = A.st32[m.off_st + i];
+    const int nq = (m.nxi + 1) / 2, H = m.P / 2 + 1;
+    EnsSmem S;
+    S.Z = reinterpret_cast<float2*>(sm);
+    S.X = S.Z + (size_t)nq * m.P;
+    S.tw = S.X + (size_t)m.nxi * H;
+    for (int t = threadIdx.x; t < m.P / 2; t += BS) {
+        double sn, cs;
+        sincospi(2.0 * t / m.P, &sn, &cs);
+        S.tw[t] = make_float2((float)cs, (float)-sn);
+    }
     __syncthreads();
     const long long o3 = 3 * m.off_n;
     double* u = A.u + o3;
@@ -126,7 +216,7 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
     double* y = A.y + o3;
     double* un = A.un + o3;
     if (!m.started) {  // FSAL seed
-        ens_rhs<BS>(m, A, st_s, rv_s, u, kk[0]);
+        ens_rhs<BS>(m, A, S, u, kk[0]);
         if (threadIdx.x == 0) M.started = 1;
     }
     for (int step = 0; step < A.budget; ++step) {
@@ -143,7 +233,7 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
                 dst[i] = u[i] + dt * acc;
             }
             __syncthreads();
-            ens_rhs<BS>(m, A, st_s, rv_s, dst, kk[s]);
+            ens_rhs<BS>(m, A, S, dst, kk[s]);
         }
         double ss = 0.0;
         int bad = 0;
@@ -222,11 +312,12 @@ struct gbc_ensemble {
     std::vector<EnsModel> host;
     std::vector<int> has_gf, has_props;
     long long total_n = 0, total_st = 0;
-    int max_nst = 0, max_n = 0;
+    size_t smem = 0;
     cudaStream_t stream = nullptr;
     EnsModel* d_models = nullptr;
-    float* st32 = nullptr;
-    double *a = nullptr, *b = nullptr, *L = nullptr, *sig = nullptr, *u = nullptr, *y = nullptr, *un = nullptr;
+    float* ghat = nullptr;
+    double *a = nullptr, *b = nullptr, *L = nullptr, *sig = nullptr, *c1 = nullptr, *u = nullptr, *y = nullptr,
+           *un = nullptr;
     double* k[7] = {};
     int block = 256;
     int log_theta = 1;
@@ -242,7 +333,7 @@ int launch_gf_ff(const FaultDev& f, double lambda, double mu, int ftype, int nre
 
 static int ens_free(gbc_ensemble* e) {
     if (e->exec) cudaGraphExecDestroy(e->exec);
-    void* ptrs[] = {e->d_models, e->st32, e->a, e->b, e->L, e->sig, e->u, e->y, e->un};
+    void* ptrs[] = {e->d_models, e->ghat, e->a, e->b, e->L, e->sig, e->c1, e->u, e->y, e->un};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int s = 0; s < 7; ++s)
@@ -251,9 +342,20 @@ static int ens_free(gbc_ensemble* e) {
     return 0;
 }
 
-__global__ void k_f64_to_f32(const double* __restrict__ a, float* __restrict__ b, long long n) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        b[i] = (float)a[i];
+// Real spectrum of the symmetric circulant embedding of each Toeplitz column block (length P):
+// G[j,l,f] = st[0,j,l] + 2 sum_{m=1}^{nx-1} st[m,j,l] cos(2 pi f m / P), computed in FP64.
+__global__ void k_ghat(const double* __restrict__ st, int nx, int nxi, int P, float* __restrict__ g) {
+    const int H = P / 2 + 1;
+    const long long total = (long long)nxi * nxi * H;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        const int f = (int)(t % H);
+        const long long jl = t / H;  // j * nxi + l
+        const int j = (int)(jl / nxi), l = (int)(jl % nxi);
+        const double* col = st + (size_t)nx * (j + (size_t)nxi * l);
+        double acc = col[0];
+        for (int m = 1; m < nx; ++m) acc += 2.0 * col[m] * cospi(2.0 * (double)(((long long)f * m) % P) / P);
+        g[t] = (float)acc;
+    }
 }
 
 namespace gbc {
@@ -276,20 +378,24 @@ int gbc_ensemble_create(int nmodels, const int* nx, const int* nxi, gbc_ensemble
     e->has_props.assign(nmodels, 0);
     long long on = 0, os = 0;
     for (int i = 0; i < nmodels; ++i) {
-        if (nx[i] <= 0 || nxi[i] <= 0) { delete e; return fail(GBC_EINVAL, "model sizes must be positive"); }
+        if (nx[i] <= 0 || nxi[i] <= 0 || nx[i] > 4096 || nxi[i] > 64) {
+            delete e;
+            return fail(GBC_EINVAL, "ensemble model sizes must satisfy 0 < nx <= 4096, 0 < nxi <= 64");
+        }
         EnsModel& m = e->host[i];
         memset(&m, 0, sizeof(m));
         m.nx = nx[i]; m.nxi = nxi[i]; m.N = nx[i] * nxi[i];
+        m.P = 2; m.logP = 1;
+        while (m.P < 2 * nx[i] - 1) { m.P <<= 1; ++m.logP; }
         m.off_n = on; m.off_st = os;
         on += m.N;
-        os += (long long)nx[i] * nxi[i] * nxi[i];
-        e->max_nst = std::max(e->max_nst, nx[i] * nxi[i] * nxi[i]);
-        e->max_n = std::max(e->max_n, m.N);
+        os += (long long)nxi[i] * nxi[i] * (m.P / 2 + 1);
+        const size_t sm = sizeof(float) * 2 * ((size_t)((nxi[i] + 1) / 2) * m.P + (size_t)nxi[i] * (m.P / 2 + 1) + m.P / 2);
+        e->smem = std::max(e->smem, sm);
     }
     e->total_n = on;
     e->total_st = os;
-    const size_t smem = sizeof(float) * ((size_t)e->max_nst + e->max_n);
-    if (smem > 200 * 1024) { delete e; return fail(GBC_EINVAL, "largest ensemble model exceeds the shared-memory budget (nx*nxi*nxi + nx*nxi floats <= 200 KB)"); }
+    if (e->smem > 200 * 1024) { delete e; return fail(GBC_EINVAL, "largest ensemble model exceeds the 200 KB shared-memory budget of its FFT buffers"); }
     int rc = 0;
     cudaError_t ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
     if (ce != cudaSuccess) rc = cuda_fail(ce, "cudaStreamCreate");
@@ -299,8 +405,8 @@ int gbc_ensemble_create(int nmodels, const int* nx, const int* nxi, gbc_ensemble
         if (c2 != cudaSuccess) rc = cuda_fail(c2, "cudaMalloc");
     };
     A((void**)&e->d_models, sizeof(EnsModel) * nmodels);
-    A((void**)&e->st32, sizeof(float) * os);
-    for (double** p : {&e->a, &e->b, &e->L, &e->sig}) A((void**)p, sizeof(double) * on);
+    A((void**)&e->ghat, sizeof(float) * os);
+    for (double** p : {&e->a, &e->b, &e->L, &e->sig, &e->c1}) A((void**)p, sizeof(double) * on);
     for (double** p : {&e->u, &e->y, &e->un}) A((void**)p, sizeof(double) * 3 * on);
     for (int s = 0; s < 7; ++s) A((void**)&e->k[s], sizeof(double) * 3 * on);
     if (rc) { ens_free(e); delete e; return rc; }
@@ -343,7 +449,7 @@ int gbc_ensemble_set_gf(gbc_ensemble* e, int model, int which, const double* hos
         rc = fail(GBC_EINVAL, "ensembles hold fault-only models (GBC_GF11_REAL or GBC_GF11_DFT)");
     }
     if (!rc) {
-        k_f64_to_f32<<<64, 256, 0, e->stream>>>(d2, e->st32 + m.off_st, (long long)nst);
+        k_ghat<<<64, 256, 0, e->stream>>>(d2, m.nx, m.nxi, m.P, e->ghat + m.off_st);
         count_launches(1);
         cudaError_t c = cudaStreamSynchronize(e->stream);
         if (c != cudaSuccess) rc = cuda_fail(c, "cudaStreamSynchronize");
@@ -386,7 +492,7 @@ int gbc_ensemble_assemble(gbc_ensemble* e, int model, const gbc_fault_mesh* mf, 
         rc = launch_gf_ff(f, lambda, mu, ftype, nrept, buffer_ratio, st, e->stream);
     }
     if (!rc) {
-        k_f64_to_f32<<<64, 256, 0, e->stream>>>(st, e->st32 + m.off_st, (long long)nst);
+        k_ghat<<<64, 256, 0, e->stream>>>(st, m.nx, m.nxi, m.P, e->ghat + m.off_st);
         count_launches(2);
         cudaError_t c = cudaStreamSynchronize(e->stream);
         if (c != cudaSuccess) rc = cuda_fail(c, "cudaStreamSynchronize");
@@ -406,6 +512,9 @@ int gbc_ensemble_set_fault_props(gbc_ensemble* e, int model, const double* a, co
     GBC_CUDA(cudaMemcpyAsync(e->b + m.off_n, b, sizeof(double) * N, cudaMemcpyHostToDevice, e->stream));
     GBC_CUDA(cudaMemcpyAsync(e->L + m.off_n, L, sizeof(double) * N, cudaMemcpyHostToDevice, e->stream));
     GBC_CUDA(cudaMemcpyAsync(e->sig + m.off_n, sigma, sizeof(double) * N, cudaMemcpyHostToDevice, e->stream));
+    std::vector<double> c1(N);
+    for (size_t i = 0; i < N; ++i) c1[i] = f0 / a[i] + (b[i] / a[i]) * std::log(v0 / L[i]) - std::log(2.0 * v0);
+    GBC_CUDA(cudaMemcpyAsync(e->c1 + m.off_n, c1.data(), sizeof(double) * N, cudaMemcpyHostToDevice, e->stream));
     GBC_CUDA(cudaStreamSynchronize(e->stream));
     m.eta = eta; m.vpl = vpl; m.f0 = f0; m.v0 = v0;
     e->has_props[model] = 1;
@@ -425,7 +534,7 @@ int gbc_ensemble_set_log_theta(gbc_ensemble* e, int on) {
 }
 
 static int ens_launch(gbc_ensemble* e, const EnsArgs& A, int block, cudaStream_t s) {
-    const size_t smem = sizeof(float) * ((size_t)e->max_nst + e->max_n);
+    const size_t smem = e->smem;
     switch (block) {
         case 128:
             GBC_CUDA(cudaFuncSetAttribute(k_ensemble<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -470,8 +579,8 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
     GBC_CUDA(cudaMemcpyAsync(e->d_models, e->host.data(), sizeof(EnsModel) * e->n, cudaMemcpyHostToDevice, s));
     if (u_dev != e->u) GBC_CUDA(cudaMemcpyAsync(e->u, u_dev, sizeof(double) * 3 * e->total_n, cudaMemcpyDeviceToDevice, s));
     EnsArgs A{};
-    A.models = e->d_models; A.nmodels = e->n; A.st32 = e->st32;
-    A.a = e->a; A.b = e->b; A.L = e->L; A.sig = e->sig;
+    A.models = e->d_models; A.nmodels = e->n; A.ghat = e->ghat;
+    A.a = e->a; A.b = e->b; A.L = e->L; A.sig = e->sig; A.c1 = e->c1;
     A.u = e->u; for (int k = 0; k < 7; ++k) A.k[k] = e->k[k];
     A.y = e->y; A.un = e->un;
     A.reltol = o->reltol; A.abstol = o->abstol; A.dtmax = o->dtmax; A.dtmin = o->dtmin;
