@@ -206,6 +206,56 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
                                const gbc_solver_opts* opts, gbc_solver_stats* stats);
 void* gbc_ensemble_stream(gbc_ensemble* e);
 
+/* ---- Serving: continuous batching of cycle-simulation requests on one GPU ------------------ */
+
+typedef struct gbc_server gbc_server;
+
+/* One request: a fault (and optionally a mantle) with its properties, initial state and horizon.
+ * Every array is copied at submission. Fault-only requests run in the server's continuous batch
+ * with the server's solver options; mantle requests run on their own stream with block-scaled
+ * `precision` Green's functions (GBC_PREC_BF16/F16, or F64) and their own options when
+ * ne_opts_valid is set. u0 is (v, θ, δ) or (v, θ, ϵ, σ, δ). */
+typedef struct gbc_request {
+    const gbc_fault_mesh* mf;
+    const gbc_hex_mesh* ma;         /* NULL: fault-only */
+    double lambda, mu;
+    int ftype, nrept;
+    double buffer_ratio;
+    const double *a, *b, *L, *sigma;
+    double eta, vpl, f0, v0;
+    const double *gamma, *n, *deps0; /* mantle requests only */
+    const double *qcoords, *qweights;
+    int nq;
+    const double* u0;
+    double t0, t1;
+    int precision;
+    int ne_opts_valid;
+    gbc_solver_opts opts;
+} gbc_request;
+
+typedef struct gbc_request_result {
+    long long id;
+    int status;
+    double submit_s, admit_s, done_s; /* seconds since the server started */
+    gbc_solver_stats stats;
+} gbc_request_result;
+
+typedef struct gbc_server_info {
+    int queued, batched, mantle;
+    double bytes_in_use, peak_bytes;
+    long long iterations;
+} gbc_server_info;
+
+/* A server admitting requests while their estimated device footprint fits hbm_budget_bytes
+ * (arrival order). A native scheduler thread owns all GPU work. */
+int gbc_server_create(double hbm_budget_bytes, const gbc_solver_opts* batch_opts, gbc_server** out);
+int gbc_server_submit(gbc_server* s, const gbc_request* req, long long* id);
+/* Blocks until request id finishes; writes its final state into u_out (host, may be NULL). */
+int gbc_server_wait(gbc_server* s, long long id, double* u_out, gbc_request_result* res);
+int gbc_server_query(gbc_server* s, gbc_server_info* out);
+/* Finishes every admitted and queued request, then stops the scheduler. */
+void gbc_server_destroy(gbc_server* s);
+
 /* ---- Diagnostics ------------------------------------------------------------------------ */
 int gbc_last_error(char* buf, size_t len);
 const char* gbc_version(void);

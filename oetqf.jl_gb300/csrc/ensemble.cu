@@ -16,35 +16,10 @@
 #include <string>
 #include <vector>
 
+#include "ensemble.cuh"
 #include "gbc_internal.cuh"
 
 namespace gbc {
-
-struct EnsModel {
-    int nx, nxi, N, log_theta;
-    int P, logP;       // FFT length (power of two >= 2nx - 1) and its log2
-    long long off_n;   // patch offset (props); state offset is 3 * off_n
-    long long off_st;  // offset into the real spectra ghat: (nxi, nxi, P/2 + 1) floats
-    double eta, vpl, f0, v0;
-    double t, dt, t1, qold;
-    long long naccept, nreject, iters, maxiters;
-    int status, done, started, logged;  // logged: θ slot holds ln θ during this integration
-};
-
-struct EnsArgs {
-    EnsModel* models;
-    int nmodels;
-    const float* ghat;           // real spectra of the symmetric circulant kernels
-    const double *a, *b, *L, *sig;
-    const double* c1;            // f0/a + (b/a) ln(v0/L) - ln(2 v0): ln ψ1 = c1 + (b/a) ln θ
-    double* u;
-    double* k[7];
-    double* y;
-    double* un;
-    double reltol, abstol, dtmax, dtmin;
-    int budget;                      // step cap per launch and model
-    unsigned long long budget_ns;    // wall-clock budget per launch (all models stay busy until done)
-};
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
@@ -130,7 +105,7 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
     __syncthreads();
     // Y_j[f] = sum_l G[j,l,f] X_l[f] (G real); repack (2q, 2q+1) as Y_2q + i Y_2q+1 with Hermitian fill,
     // bit-reversed for the inverse transform
-    const float* G = A.ghat + m.off_st;
+    const float* G = m.ghat;
     for (int t = threadIdx.x; t < nq * H; t += BS) {
         const int q = t / H, f = t - q * H;
         const int j0 = 2 * q, j1 = 2 * q + 1;
@@ -154,11 +129,11 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
     __syncthreads();
     fft_many<BS>(S.Z, nq, P, logP, S.tw, 1);
     const double invP = 1.0 / P;
-    const double* pa = A.a + m.off_n;
-    const double* pb = A.b + m.off_n;
-    const double* pL = A.L + m.off_n;
-    const double* ps = A.sig + m.off_n;
-    const double* pc = A.c1 + m.off_n;
+    const double* pa = m.a;
+    const double* pb = m.b;
+    const double* pL = m.L;
+    const double* ps = m.sig;
+    const double* pc = m.c1;
     for (int i = threadIdx.x; i < N; i += BS) {
         const int ii = i % nx, j = i / nx;
         const float2 w = S.Z[(j >> 1) * P + ii];
@@ -209,12 +184,11 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
         S.tw[t] = make_float2((float)cs, (float)-sn);
     }
     __syncthreads();
-    const long long o3 = 3 * m.off_n;
-    double* u = A.u + o3;
+    double* u = m.u;
     double* kk[7];
-    for (int s = 0; s < 7; ++s) kk[s] = A.k[s] + o3;
-    double* y = A.y + o3;
-    double* un = A.un + o3;
+    for (int s = 0; s < 7; ++s) kk[s] = m.k[s];
+    double* y = m.y;
+    double* un = m.un;
     if (!m.started) {  // FSAL seed
         ens_rhs<BS>(m, A, S, u, kk[0]);
         if (threadIdx.x == 0) M.started = 1;
@@ -296,10 +270,54 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
     }
 }
 
+__global__ void k_ens_theta(EnsArgs A, int to_log);
+
+int ens_prepare_model(EnsModel& m, int nx, int nxi, size_t* smem_bytes) {
+    if (nx <= 0 || nxi <= 0 || nx > 4096 || nxi > 64)
+        return fail(GBC_EINVAL, "ensemble model sizes must satisfy 0 < nx <= 4096, 0 < nxi <= 64");
+    memset(&m, 0, sizeof(m));
+    m.nx = nx; m.nxi = nxi; m.N = nx * nxi;
+    m.P = 2; m.logP = 1;
+    while (m.P < 2 * nx - 1) { m.P <<= 1; ++m.logP; }
+    *smem_bytes = sizeof(float) * 2 * ((size_t)((nxi + 1) / 2) * m.P + (size_t)nxi * (m.P / 2 + 1) + m.P / 2);
+    if (*smem_bytes > 200 * 1024) return fail(GBC_EINVAL, "model exceeds the 200 KB shared-memory budget of its FFT buffers");
+    return 0;
+}
+
+size_t ens_ghat_floats(const EnsModel& m) { return (size_t)m.nxi * m.nxi * (m.P / 2 + 1); }
+
+__global__ void k_ghat(const double* __restrict__ st, int nx, int nxi, int P, float* __restrict__ g);
+
+int ens_ghat(const double* st_dev, const EnsModel& m, float* ghat_dev, cudaStream_t s) {
+    k_ghat<<<64, 256, 0, s>>>(st_dev, m.nx, m.nxi, m.P, ghat_dev);
+    GBC_CUDA(cudaGetLastError());
+    return 0;
+}
+
+static int ens_launch_block(EnsModel* d_models, int n, const EnsArgs& A0, int block, size_t smem, cudaStream_t s);
+
+int ens_run(EnsModel* d_models, int n, double reltol, double abstol, double dtmax, double dtmin,
+            unsigned long long budget_ns, int block, size_t smem, cudaStream_t s) {
+    EnsArgs A{};
+    A.models = d_models; A.nmodels = n;
+    A.reltol = reltol; A.abstol = abstol; A.dtmax = dtmax; A.dtmin = dtmin;
+    A.budget = 1 << 20;
+    A.budget_ns = budget_ns;
+    return ens_launch_block(d_models, n, A, block, smem, s);
+}
+
+int ens_theta(EnsModel* d_models, int n, int to_log, cudaStream_t s) {
+    EnsArgs A{};
+    A.models = d_models; A.nmodels = n;
+    k_ens_theta<<<n, 256, 0, s>>>(A, to_log);
+    GBC_CUDA(cudaGetLastError());
+    return 0;
+}
+
 __global__ void k_ens_theta(EnsArgs A, int to_log) {
     const EnsModel& m = A.models[blockIdx.x];
     if (!m.logged) return;  // models with nothing to integrate keep θ untouched
-    double* th = A.u + 3 * m.off_n + m.N;
+    double* th = m.u + m.N;
     for (int i = threadIdx.x; i < m.N; i += blockDim.x) th[i] = to_log ? log(th[i]) : exp(th[i]);
 }
 
@@ -326,7 +344,6 @@ struct gbc_ensemble {
 };
 
 namespace gbc {
-void count_launches(long long n);
 int launch_gf_ff(const FaultDev& f, double lambda, double mu, int ftype, int nrept, double buffer_ratio, double* st,
                  cudaStream_t s);
 }
@@ -342,6 +359,7 @@ static int ens_free(gbc_ensemble* e) {
     return 0;
 }
 
+namespace gbc {
 // Real spectrum of the symmetric circulant embedding of each Toeplitz column block (length P):
 // G[j,l,f] = st[0,j,l] + 2 sum_{m=1}^{nx-1} st[m,j,l] cos(2 pi f m / P), computed in FP64.
 __global__ void k_ghat(const double* __restrict__ st, int nx, int nxi, int P, float* __restrict__ g) {
@@ -358,8 +376,35 @@ __global__ void k_ghat(const double* __restrict__ st, int nx, int nxi, int P, fl
     }
 }
 
+}  // namespace gbc
+
 namespace gbc {
 int launch_gf_ff_idft(int nx, int nxi, const double* st_dft, double* st, cudaStream_t s);
+}
+
+namespace gbc {
+static int ens_launch_block(EnsModel* d_models, int n, const EnsArgs& A, int block, size_t smem, cudaStream_t s) {
+    (void)d_models;
+    switch (block) {
+        case 128:
+            GBC_CUDA(cudaFuncSetAttribute(k_ensemble<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_ensemble<128><<<n, 128, smem, s>>>(A);
+            break;
+        case 512:
+            GBC_CUDA(cudaFuncSetAttribute(k_ensemble<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_ensemble<512><<<n, 512, smem, s>>>(A);
+            break;
+        default:
+            GBC_CUDA(cudaFuncSetAttribute(k_ensemble<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_ensemble<256><<<n, 256, smem, s>>>(A);
+    }
+    GBC_CUDA(cudaGetLastError());
+    return 0;
+}
+}  // namespace gbc
+
+static int ens_launch(gbc_ensemble* e, const EnsArgs& A, int block, cudaStream_t s) {
+    return ens_launch_block(e->d_models, e->n, A, block, e->smem, s);
 }
 
 extern "C" {
@@ -410,6 +455,12 @@ int gbc_ensemble_create(int nmodels, const int* nx, const int* nxi, gbc_ensemble
     for (double** p : {&e->u, &e->y, &e->un}) A((void**)p, sizeof(double) * 3 * on);
     for (int s = 0; s < 7; ++s) A((void**)&e->k[s], sizeof(double) * 3 * on);
     if (rc) { ens_free(e); delete e; return rc; }
+    for (EnsModel& m : e->host) {
+        m.ghat = e->ghat + m.off_st;
+        m.a = e->a + m.off_n; m.b = e->b + m.off_n; m.L = e->L + m.off_n; m.sig = e->sig + m.off_n; m.c1 = e->c1 + m.off_n;
+        m.u = e->u + 3 * m.off_n; m.y = e->y + 3 * m.off_n; m.un = e->un + 3 * m.off_n;
+        for (int s = 0; s < 7; ++s) m.k[s] = e->k[s] + 3 * m.off_n;
+    }
     *out = e;
     return 0;
 }
@@ -533,24 +584,6 @@ int gbc_ensemble_set_log_theta(gbc_ensemble* e, int on) {
     return 0;
 }
 
-static int ens_launch(gbc_ensemble* e, const EnsArgs& A, int block, cudaStream_t s) {
-    const size_t smem = e->smem;
-    switch (block) {
-        case 128:
-            GBC_CUDA(cudaFuncSetAttribute(k_ensemble<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_ensemble<128><<<e->n, 128, smem, s>>>(A);
-            break;
-        case 512:
-            GBC_CUDA(cudaFuncSetAttribute(k_ensemble<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_ensemble<512><<<e->n, 512, smem, s>>>(A);
-            break;
-        default:
-            GBC_CUDA(cudaFuncSetAttribute(k_ensemble<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_ensemble<256><<<e->n, 256, smem, s>>>(A);
-    }
-    GBC_CUDA(cudaGetLastError());
-    return 0;
-}
 
 // Integrates every model (or only those with active != 0 when given) from its current state to its
 // own t1; state u is the concatenation of the models' (v, θ, δ) on the device.
@@ -579,10 +612,7 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
     GBC_CUDA(cudaMemcpyAsync(e->d_models, e->host.data(), sizeof(EnsModel) * e->n, cudaMemcpyHostToDevice, s));
     if (u_dev != e->u) GBC_CUDA(cudaMemcpyAsync(e->u, u_dev, sizeof(double) * 3 * e->total_n, cudaMemcpyDeviceToDevice, s));
     EnsArgs A{};
-    A.models = e->d_models; A.nmodels = e->n; A.ghat = e->ghat;
-    A.a = e->a; A.b = e->b; A.L = e->L; A.sig = e->sig; A.c1 = e->c1;
-    A.u = e->u; for (int k = 0; k < 7; ++k) A.k[k] = e->k[k];
-    A.y = e->y; A.un = e->un;
+    A.models = e->d_models; A.nmodels = e->n;
     A.reltol = o->reltol; A.abstol = o->abstol; A.dtmax = o->dtmax; A.dtmin = o->dtmin;
     A.budget = 1 << 20;
     A.budget_ns = 250000000ull;  // 250 ms per launch

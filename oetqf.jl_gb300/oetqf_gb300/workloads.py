@@ -8,6 +8,9 @@ Random draws come from one splitmix64 stream (seeded) so CPU and GPU see identic
     γ = 1/(2η_v), n = 0) spanning 10-30 km depth, with lognormal Dc (median 12 mm, σ_ln 0.3).
   * large_fault_with_mantle(): 256 x 16 patches at 0.5 km (4096) over 40 x 20 x 10 = 8000 cells
     (x over the fault length, y over 40 km centred, 10-30 km depth), same friction, 200 years.
+  * serving_requests(): cycle-simulation requests with 500-4096 patches (10 rows, 1 km cells),
+    an optional mantle of 0-4000 cells (a box under the fault, 10-30 km depth) and horizons of
+    10-200 years; friction as in fault_ensemble().
   * fault_ensemble(): independent fault-only models with N ~ U[200, 2000] patches (10 rows of
     1 km cells, nx = round(N/10)); per model a - b ~ U(-0.006, 0.004) on the 2-8 km zone (a = 0.015
     there, 0.025 / b = 0.019 elsewhere), Dc lognormal (median 10 mm, σ_ln 0.3), σ ~ U(30, 80) MPa.
@@ -129,4 +132,28 @@ def fault_ensemble(n_models=256, years=50.0, seed=3, n_range=(200, 2000), nxi=10
         th0 = pf.L.reshape(-1, order="F") / VPL * (1 + 0.01 * (2 * rng.uniform(Nn) - 1))
         u0 = np.concatenate([np.full(Nn, VPL), th0, np.zeros(Nn)])
         out.append(CycleModel(mf, None, pf, None, u0, years * YEAR, name=f"ensemble member {m} ({mf.nx}x{mf.nξ})"))
+    return out
+
+
+def serving_requests(n_requests=32, seed=5, mantle_fraction=0.25, patch_range=(500, 4096), cell_range=(0, 4000),
+                     year_range=(10.0, 200.0)) -> list[CycleModel]:
+    rng = SplitMix64(seed)
+    out = []
+    for r in range(n_requests):
+        N = patch_range[0] + (patch_range[1] - patch_range[0]) * rng.uniform(1)[0]
+        years = year_range[0] + (year_range[1] - year_range[0]) * rng.uniform(1)[0]
+        member = fault_ensemble(n_models=1, years=years, seed=int(rng.next_u64() % 1000003), n_range=(N, N))[0]
+        if rng.uniform(1)[0] < mantle_fraction:
+            ne_target = max(1, int(cell_range[0] + (cell_range[1] - cell_range[0]) * rng.uniform(1)[0]))
+            nz = 4
+            nxy = max(1, int(round((ne_target / nz) ** 0.5)))
+            L = member.mf.nx * 1e3
+            ma = gen_hex8_box(-L / 2, -L / 4, -10e3, L, L / 2, -20e3, nxy, nxy, nz)
+            pa = PowerLawViscosityProperty(np.full(ma.ne, 1.0 / (2.0 * 1e19)), np.zeros(ma.ne), np.zeros(6))
+            Nn = member.N
+            u0 = np.concatenate([member.u0[:2 * Nn], np.zeros(12 * ma.ne), member.u0[2 * Nn:]])
+            member = CycleModel(member.mf, ma, member.pf, pa, u0, member.horizon, name=f"request {r} (+mantle {ma.ne})")
+        else:
+            member.name = f"request {r}"
+        out.append(member)
     return out

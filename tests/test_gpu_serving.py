@@ -1,0 +1,68 @@
+"""Serving: continuous batching with HBM-budget admission; each result is the same alone and in
+the mix (bitwise: every model's kernels and step control are independent of its neighbours)."""
+import numpy as np
+import pytest
+
+from oetqf_gb300.workloads import YEAR, fault_ensemble, serving_requests
+
+pytestmark = pytest.mark.gpu
+
+
+def _mix():
+    reqs = serving_requests(n_requests=6, seed=11, mantle_fraction=0.34, patch_range=(100, 600), cell_range=(8, 64),
+                            year_range=(0.5, 2.0))
+    assert any(r.ma is not None for r in reqs) and any(r.ma is None for r in reqs)
+    return reqs
+
+
+def test_alone_equals_in_the_mix():
+    from oetqf_gb300.serving import Server, run_stream
+    reqs = _mix()
+    s = Server(hbm_budget_gb=8.0)
+    out = run_stream(s, reqs, rate_per_s=50.0, seed=1)
+    s.close()
+    assert out["status"] == [0]
+    for i in (0, 1, 2, 3, 4, 5):
+        alone = Server(hbm_budget_gb=8.0)
+        rid = alone.submit(reqs[i])
+        u_alone, res = alone.wait(rid)
+        alone.close()
+        u_mix = out["results"][i][0]
+        np.testing.assert_array_equal(u_alone, u_mix)
+        assert res.stats.t == pytest.approx(reqs[i].horizon)
+
+
+def test_budget_admission_limits_concurrency():
+    from oetqf_gb300.serving import Server
+    reqs = fault_ensemble(n_models=6, years=0.5, n_range=(300, 400), seed=13)
+    budget_gb = 0.0004  # each request needs about 160 KB: two fit at a time
+    s = Server(hbm_budget_gb=budget_gb)
+    ids = [s.submit(r) for r in reqs]
+    results = [s.wait(i) for i in ids]
+    info = s.info()
+    s.close()
+    assert all(r.status == 0 for _, r in results)
+    assert 0 < info.peak_bytes <= budget_gb * 2**30
+    admits = sorted(r.admit_s for _, r in results)
+    dones = sorted(r.done_s for _, r in results)
+    assert admits[-1] >= dones[0]  # the last request waited for memory to free up
+
+
+def test_server_matches_standalone_ensemble():
+    from oetqf_gb300.ensemble import Ensemble
+    from oetqf_gb300.serving import Server
+    reqs = fault_ensemble(n_models=3, years=1.0, n_range=(80, 300), seed=17)
+    s = Server(hbm_budget_gb=4.0)
+    ids = [s.submit(r) for r in reqs]
+    got = [s.wait(i)[0] for i in ids]
+    s.close()
+    e = Ensemble([(r.mf.nx, r.mf.nξ) for r in reqs])
+    u0 = np.zeros(e.state_len)
+    for i, r in enumerate(reqs):
+        e.assemble(i, r.mf, r.lam, r.mu)
+        e.set_fault_props(i, r.pf)
+        u0[e.offsets[i]:e.offsets[i] + r.u0.size] = r.u0
+    e.set_block(512)
+    u, st = e.integrate(u0, 0.0, [r.horizon for r in reqs])
+    for i, r in enumerate(reqs):
+        np.testing.assert_array_equal(got[i], u[e.offsets[i]:e.offsets[i] + r.u0.size])
