@@ -195,6 +195,11 @@ int gbc_ensemble_set_fault_props(gbc_ensemble* e, int model, const double* a, co
 int gbc_ensemble_set_block(gbc_ensemble* e, int threads);
 /* Integrate ψ = ln θ internally (default on; the caller's state keeps θ). */
 int gbc_ensemble_set_log_theta(gbc_ensemble* e, int on);
+/* Largest thread-block cluster per model (1, 2, 4 or 8; default 8). Models above 600 patches
+ * are split over a cluster of CTAs (2 up to 1200 patches, 4 up to 2400, 8 beyond): each CTA owns
+ * a slice of the patches for the friction update, the stages and the error norm, and the CTAs
+ * meet at cluster barriers. */
+int gbc_ensemble_set_max_cluster(gbc_ensemble* e, int ctas);
 /* The flat state is the concatenation over models of (v, θ, δ); model i starts at
  * gbc_ensemble_state_offset(e, i). Each model integrates from t0[i] to t1[i]; stats has one entry
  * per model. The _dev variant takes a device pointer. */

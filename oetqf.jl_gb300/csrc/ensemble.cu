@@ -8,6 +8,7 @@
 // Reference: the fault-only ode (src/BEM/equation.jl:156-166) = relative_velocity! (:35-42),
 // dτ_dt! (:44-61, applied as the direct Toeplitz sum), update_fault! (:233-246) and the ageing
 // law (:279); the integrator stands in for OrdinaryDiffEq's solve (src/io.jl:125-130).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -78,7 +79,10 @@ __device__ __forceinline__ void fft_many(float2* Z, int nq, int P, int logP, con
 // rows per inverse FFT.
 template <int BS>
 __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, const EnsSmem& S,
-                                        const double* __restrict__ y, double* __restrict__ k) {
+                                        const double* __restrict__ y, double* __restrict__ k, int lo, int hi,
+                                        cooperative_groups::cluster_group& cl) {
+    // every rank's slice of y (the stage state) must be visible before the full slip-rate vector is read
+    cl.sync();
     const int N = m.N, nx = m.nx, nxi = m.nxi, P = m.P, logP = m.logP, H = P / 2 + 1;
     const int nq = (nxi + 1) / 2;
     const double* v = y;
@@ -134,7 +138,7 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
     const double* pL = m.L;
     const double* ps = m.sig;
     const double* pc = m.c1;
-    for (int i = threadIdx.x; i < N; i += BS) {
+    for (int i = lo + threadIdx.x; i < hi; i += BS) {
         const int ii = i % nx, j = i / nx;
         const float2 w = S.Z[(j >> 1) * P + ii];
         const double dtau = (double)((j & 1) ? w.y : w.x) * invP;
@@ -161,18 +165,32 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
     __syncthreads();
 }
 
+namespace cg = cooperative_groups;
+
+// per-CTA copy of the model's step control; every CTA of a cluster computes it identically and
+// cluster rank 0 writes it back to the descriptor
+struct EnsCtl {
+    double t, dt, t1, qold;
+    long long naccept, nreject, iters, maxiters;
+    int done, status, go, stop;
+};
+
 template <int BS>
 __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
     extern __shared__ __align__(16) float sm[];
     __shared__ double red[BS / 32];
-    __shared__ int s_go, s_stop;
+    __shared__ EnsCtl c;
+    cg::cluster_group cl = cg::this_cluster();
+    const int csize = (int)cl.num_blocks();
+    const int rank = (int)cl.block_rank();
     const unsigned long long t_launch = global_ns();
-    const int mi = blockIdx.x;
-    if (mi >= A.nmodels) return;
+    const int slot = A.first + (int)(blockIdx.x / csize);
+    const int mi = A.order ? A.order[slot] : slot;
     EnsModel& M = A.models[mi];
-    if (M.done) return;
-    const EnsModel m = M;  // sizes and constants (t, dt live in M)
-    const int N = m.N, n3 = 3 * N;
+    const EnsModel m = M;  // sizes, constants and the step control state at launch
+    if (m.done) return;    // the same descriptor for every rank: cluster-uniform
+    const int N = m.N;
+    const int lo = (int)((long long)N * rank / csize), hi = (int)((long long)N * (rank + 1) / csize);
     const int nq = (m.nxi + 1) / 2, H = m.P / 2 + 1;
     EnsSmem S;
     S.Z = reinterpret_cast<float2*>(sm);
@@ -183,45 +201,56 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
         sincospi(2.0 * t / m.P, &sn, &cs);
         S.tw[t] = make_float2((float)cs, (float)-sn);
     }
+    if (threadIdx.x == 0) {
+        c.t = m.t; c.dt = m.dt; c.t1 = m.t1; c.qold = m.qold;
+        c.naccept = m.naccept; c.nreject = m.nreject; c.iters = m.iters; c.maxiters = m.maxiters;
+        c.done = m.done; c.status = m.status; c.go = 0; c.stop = 0;
+    }
     __syncthreads();
     double* u = m.u;
     double* kk[7];
     for (int s = 0; s < 7; ++s) kk[s] = m.k[s];
     double* y = m.y;
     double* un = m.un;
+    const bool writer = (rank == 0 && threadIdx.x == 0);
     if (!m.started) {  // FSAL seed
-        ens_rhs<BS>(m, A, S, u, kk[0]);
-        if (threadIdx.x == 0) M.started = 1;
+        ens_rhs<BS>(m, A, S, u, kk[0], lo, hi, cl);
+        if (writer) M.started = 1;
     }
     for (int step = 0; step < A.budget; ++step) {
+        // stop decision of rank 0 (completion or the launch's wall-clock budget), shared through L2
+        if (writer) A.ctl[mi] = c.done || (global_ns() - t_launch > A.budget_ns);
+        cl.sync();
+        if (threadIdx.x == 0) c.stop = ((volatile int*)A.ctl)[mi];
         __syncthreads();
-        if (threadIdx.x == 0) s_stop = M.done || (global_ns() - t_launch > A.budget_ns);
-        __syncthreads();
-        if (s_stop) break;
-        const double dt = M.dt;
+        if (c.stop) break;
+        const double dt = c.dt;
         for (int s = 1; s < 7; ++s) {
             double* dst = (s == 6) ? un : y;
-            for (int i = threadIdx.x; i < n3; i += BS) {
-                double acc = 0.0;
-                for (int r = 0; r < s; ++r) acc = fma(e_ta[s][r], kk[r][i], acc);
-                dst[i] = u[i] + dt * acc;
-            }
-            __syncthreads();
-            ens_rhs<BS>(m, A, S, dst, kk[s]);
+            for (int comp = 0; comp < 3; ++comp)
+                for (int i = lo + threadIdx.x; i < hi; i += BS) {
+                    const int g = comp * N + i;
+                    double acc = 0.0;
+                    for (int r = 0; r < s; ++r) acc = fma(e_ta[s][r], kk[r][g], acc);
+                    dst[g] = u[g] + dt * acc;
+                }
+            ens_rhs<BS>(m, A, S, dst, kk[s], lo, hi, cl);
         }
         double ss = 0.0;
         int bad = 0;
-        for (int i = threadIdx.x; i < n3; i += BS) {
-            double e = 0.0;
+        for (int comp = 0; comp < 3; ++comp)
+            for (int i = lo + threadIdx.x; i < hi; i += BS) {
+                const int g = comp * N + i;
+                double e = 0.0;
 #pragma unroll
-            for (int s = 0; s < 7; ++s) e = fma(e_te[s], kk[s][i], e);
-            e *= dt;
-            const double unv = un[i];
-            const double sc = A.abstol + A.reltol * fmax(fabs(u[i]), fabs(unv));
-            const double r = e / sc;
-            ss = fma(r, r, ss);
-            bad |= !isfinite(unv);
-        }
+                for (int s = 0; s < 7; ++s) e = fma(e_te[s], kk[s][g], e);
+                e *= dt;
+                const double unv = un[g];
+                const double sc = A.abstol + A.reltol * fmax(fabs(u[g]), fabs(unv));
+                const double r = e / sc;
+                ss = fma(r, r, ss);
+                bad |= !isfinite(unv);
+            }
         for (int o = 16; o > 0; o >>= 1) {
             ss += __shfl_xor_sync(0xffffffffu, ss, o);
             bad |= __shfl_xor_sync(0xffffffffu, bad, o);
@@ -229,43 +258,56 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = bad ? INFINITY : ss;
         __syncthreads();
         if (threadIdx.x == 0) {
-            double tot = 0.0;
-            for (int w = 0; w < BS / 32; ++w) tot += red[w];
-            double EEst = sqrt(tot / (double)n3);
+            double part = 0.0;
+            for (int w = 0; w < BS / 32; ++w) part += red[w];
+            A.part[mi * 16 + rank] = part;
+        }
+        cl.sync();
+        if (threadIdx.x == 0) {
+            double tot = 0.0;  // same order in every rank
+            for (int r = 0; r < csize; ++r) tot += ((volatile double*)A.part)[mi * 16 + r];
+            double EEst = sqrt(tot / (double)(3 * N));
             if (!isfinite(EEst)) EEst = INFINITY;
             const double beta1 = 0.14, beta2 = 0.08, gam = 0.9, qmin = 0.2, qmax = 10.0;
             const double q11 = pow(EEst, beta1);
-            M.iters += 1;
+            c.iters += 1;
             double dtn;
             int acc = 0;
             if (EEst <= 1.0) {
-                double q = q11 / pow(M.qold, beta2);
+                double q = q11 / pow(c.qold, beta2);
                 q = fmax(1.0 / qmax, fmin(1.0 / qmin, q / gam));
-                const double tn = M.t + dt;
-                M.t = (tn >= M.t1) ? M.t1 : tn;
-                M.qold = fmax(EEst, 1e-4);
-                M.naccept += 1;
+                const double tn = c.t + dt;
+                c.t = (tn >= c.t1) ? c.t1 : tn;
+                c.qold = fmax(EEst, 1e-4);
+                c.naccept += 1;
                 acc = 1;
                 dtn = dt / q;
             } else {
                 const double q = isfinite(q11) ? fmin(1.0 / qmin, q11 / gam) : 1.0 / qmin;
-                M.nreject += 1;
+                c.nreject += 1;
                 dtn = dt / q;
             }
-            if (M.t >= M.t1) { M.done = 1; M.status = 0; }
-            else if (dtn < A.dtmin || !isfinite(dtn) || M.iters >= M.maxiters) { M.done = 1; M.status = -5; }
+            if (c.t >= c.t1) { c.done = 1; c.status = 0; }
+            else if (dtn < A.dtmin || !isfinite(dtn) || c.iters >= c.maxiters) { c.done = 1; c.status = -5; }
             if (dtn > A.dtmax) dtn = A.dtmax;
-            const double rem = M.t1 - M.t;
+            const double rem = c.t1 - c.t;
             if (dtn >= rem) dtn = rem;
-            M.dt = dtn;
-            s_go = acc;
+            c.dt = dtn;
+            c.go = acc;
+            if (rank == 0) {
+                M.t = c.t; M.dt = c.dt; M.qold = c.qold;
+                M.naccept = c.naccept; M.nreject = c.nreject; M.iters = c.iters;
+                M.done = c.done; M.status = c.status;
+            }
         }
         __syncthreads();
-        if (s_go) {
-            for (int i = threadIdx.x; i < n3; i += BS) {
-                u[i] = un[i];
-                kk[0][i] = kk[6][i];
-            }
+        if (c.go) {
+            for (int comp = 0; comp < 3; ++comp)
+                for (int i = lo + threadIdx.x; i < hi; i += BS) {
+                    const int g = comp * N + i;
+                    u[g] = un[g];
+                    kk[0][g] = kk[6][g];
+                }
         }
     }
 }
@@ -294,16 +336,103 @@ int ens_ghat(const double* st_dev, const EnsModel& m, float* ghat_dev, cudaStrea
     return 0;
 }
 
-static int ens_launch_block(EnsModel* d_models, int n, const EnsArgs& A0, int block, size_t smem, cudaStream_t s);
+int ens_csize(int N, int maxc) {
+    const int c = N <= 600 ? 1 : N <= 1200 ? 2 : N <= 2400 ? 4 : 8;
+    return c < maxc ? c : maxc;
+}
 
-int ens_run(EnsModel* d_models, int n, double reltol, double abstol, double dtmax, double dtmin,
-            unsigned long long budget_ns, int block, size_t smem, cudaStream_t s) {
+void ens_groups(const EnsModel* models, int n, int maxc, std::vector<int>& order, int first[4], int count[4]) {
+    order.clear();
+    for (int g = 0; g < 4; ++g) {
+        first[g] = (int)order.size();
+        for (int i = 0; i < n; ++i)
+            if (ens_csize(models[i].N, maxc) == (1 << g)) order.push_back(i);
+        count[g] = (int)order.size() - first[g];
+    }
+}
+
+template <int BS>
+static int launch_cluster(const EnsArgs& A, int nmod, int csize, size_t smem, cudaStream_t s) {
+    GBC_CUDA(cudaFuncSetAttribute(k_ensemble<BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(nmod * csize));
+    cfg.blockDim = dim3(BS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)csize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    GBC_CUDA(cudaLaunchKernelEx(&cfg, k_ensemble<BS>, A));
+    return 0;
+}
+
+int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtmax, double dtmin,
+                   unsigned long long budget_ns, int block, size_t smem, cudaStream_t main) {
     EnsArgs A{};
-    A.models = d_models; A.nmodels = n;
+    A.models = L.models; A.nmodels = L.n; A.order = L.order; A.part = L.part; A.ctl = L.ctl;
     A.reltol = reltol; A.abstol = abstol; A.dtmax = dtmax; A.dtmin = dtmin;
     A.budget = 1 << 20;
     A.budget_ns = budget_ns;
-    return ens_launch_block(d_models, n, A, block, smem, s);
+    GBC_CUDA(cudaEventRecord(L.fork, main));
+    int launched = 0;
+    for (int g = 0; g < 4; ++g) {
+        if (L.count[g] == 0) continue;
+        cudaStream_t s = L.aux[g];
+        GBC_CUDA(cudaStreamWaitEvent(s, L.fork, 0));
+        A.first = L.first[g];
+        int rc;
+        if (block == 128) rc = launch_cluster<128>(A, L.count[g], 1 << g, smem, s);
+        else if (block == 512) rc = launch_cluster<512>(A, L.count[g], 1 << g, smem, s);
+        else rc = launch_cluster<256>(A, L.count[g], 1 << g, smem, s);
+        if (rc) return rc;
+        GBC_CUDA(cudaEventRecord(L.join[g], s));
+        GBC_CUDA(cudaStreamWaitEvent(main, L.join[g], 0));
+        ++launched;
+    }
+    count_launches(launched);
+    return 0;
+}
+
+int ens_launch_create(EnsLaunch& L, int capacity) {
+    L = EnsLaunch();
+    L.cap = capacity;
+    GBC_CUDA(cudaMalloc(&L.order, sizeof(int) * capacity));
+    GBC_CUDA(cudaMalloc(&L.part, sizeof(double) * 16 * capacity));
+    GBC_CUDA(cudaMalloc(&L.ctl, sizeof(int) * capacity));
+    GBC_CUDA(cudaEventCreateWithFlags(&L.fork, cudaEventDisableTiming));
+    for (int g = 0; g < 4; ++g) {
+        GBC_CUDA(cudaStreamCreateWithFlags(&L.aux[g], cudaStreamNonBlocking));
+        GBC_CUDA(cudaEventCreateWithFlags(&L.join[g], cudaEventDisableTiming));
+    }
+    return 0;
+}
+
+void ens_launch_destroy(EnsLaunch& L) {
+    if (L.order) cudaFree((void*)L.order);
+    if (L.part) cudaFree(L.part);
+    if (L.ctl) cudaFree(L.ctl);
+    if (L.fork) cudaEventDestroy(L.fork);
+    for (int g = 0; g < 4; ++g) {
+        if (L.aux[g]) cudaStreamDestroy(L.aux[g]);
+        if (L.join[g]) cudaEventDestroy(L.join[g]);
+    }
+    L = EnsLaunch();
+}
+
+// uploads the grouped order of the models (host descriptors) and fills the group table
+int ens_launch_prepare(EnsLaunch& L, EnsModel* d_models, const EnsModel* host, int n, int maxc, cudaStream_t s) {
+    if (n > L.cap) return fail(GBC_EINVAL, "ensemble launch capacity exceeded");
+    std::vector<int> order;
+    ens_groups(host, n, maxc, order, L.first, L.count);
+    L.models = d_models;
+    L.n = n;
+    GBC_CUDA(cudaMemcpyAsync((void*)L.order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    GBC_CUDA(cudaStreamSynchronize(s));
+    return 0;
 }
 
 int ens_theta(EnsModel* d_models, int n, int to_log, cudaStream_t s) {
@@ -338,9 +467,11 @@ struct gbc_ensemble {
            *un = nullptr;
     double* k[7] = {};
     int block = 256;
+    int max_cluster = 8;
     int log_theta = 1;
     cudaGraphExec_t exec = nullptr;
     int exec_block = 0, exec_budget = 0;
+    EnsLaunch lp;
 };
 
 namespace gbc {
@@ -350,6 +481,7 @@ int launch_gf_ff(const FaultDev& f, double lambda, double mu, int ftype, int nre
 
 static int ens_free(gbc_ensemble* e) {
     if (e->exec) cudaGraphExecDestroy(e->exec);
+    ens_launch_destroy(e->lp);
     void* ptrs[] = {e->d_models, e->ghat, e->a, e->b, e->L, e->sig, e->c1, e->u, e->y, e->un};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -382,30 +514,6 @@ namespace gbc {
 int launch_gf_ff_idft(int nx, int nxi, const double* st_dft, double* st, cudaStream_t s);
 }
 
-namespace gbc {
-static int ens_launch_block(EnsModel* d_models, int n, const EnsArgs& A, int block, size_t smem, cudaStream_t s) {
-    (void)d_models;
-    switch (block) {
-        case 128:
-            GBC_CUDA(cudaFuncSetAttribute(k_ensemble<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_ensemble<128><<<n, 128, smem, s>>>(A);
-            break;
-        case 512:
-            GBC_CUDA(cudaFuncSetAttribute(k_ensemble<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_ensemble<512><<<n, 512, smem, s>>>(A);
-            break;
-        default:
-            GBC_CUDA(cudaFuncSetAttribute(k_ensemble<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_ensemble<256><<<n, 256, smem, s>>>(A);
-    }
-    GBC_CUDA(cudaGetLastError());
-    return 0;
-}
-}  // namespace gbc
-
-static int ens_launch(gbc_ensemble* e, const EnsArgs& A, int block, cudaStream_t s) {
-    return ens_launch_block(e->d_models, e->n, A, block, e->smem, s);
-}
 
 extern "C" {
 
@@ -454,6 +562,7 @@ int gbc_ensemble_create(int nmodels, const int* nx, const int* nxi, gbc_ensemble
     for (double** p : {&e->a, &e->b, &e->L, &e->sig, &e->c1}) A((void**)p, sizeof(double) * on);
     for (double** p : {&e->u, &e->y, &e->un}) A((void**)p, sizeof(double) * 3 * on);
     for (int s = 0; s < 7; ++s) A((void**)&e->k[s], sizeof(double) * 3 * on);
+    if (!rc) rc = ens_launch_create(e->lp, nmodels);
     if (rc) { ens_free(e); delete e; return rc; }
     for (EnsModel& m : e->host) {
         m.ghat = e->ghat + m.off_st;
@@ -578,6 +687,12 @@ int gbc_ensemble_set_block(gbc_ensemble* e, int threads) {
     return 0;
 }
 
+int gbc_ensemble_set_max_cluster(gbc_ensemble* e, int ctas) {
+    if (!e || (ctas != 1 && ctas != 2 && ctas != 4 && ctas != 8)) return fail(GBC_EINVAL, "cluster size must be 1, 2, 4 or 8");
+    e->max_cluster = ctas;
+    return 0;
+}
+
 int gbc_ensemble_set_log_theta(gbc_ensemble* e, int on) {
     if (!e) return fail(GBC_EINVAL, "null ensemble");
     e->log_theta = on ? 1 : 0;
@@ -611,24 +726,21 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
     cudaStream_t s = e->stream;
     GBC_CUDA(cudaMemcpyAsync(e->d_models, e->host.data(), sizeof(EnsModel) * e->n, cudaMemcpyHostToDevice, s));
     if (u_dev != e->u) GBC_CUDA(cudaMemcpyAsync(e->u, u_dev, sizeof(double) * 3 * e->total_n, cudaMemcpyDeviceToDevice, s));
-    EnsArgs A{};
-    A.models = e->d_models; A.nmodels = e->n;
-    A.reltol = o->reltol; A.abstol = o->abstol; A.dtmax = o->dtmax; A.dtmin = o->dtmin;
-    A.budget = 1 << 20;
-    A.budget_ns = 250000000ull;  // 250 ms per launch
+    if (int rc = ens_launch_prepare(e->lp, e->d_models, e->host.data(), e->n, e->max_cluster, s)) return rc;
     if (e->log_theta) {
-        k_ens_theta<<<e->n, 256, 0, s>>>(A, 1);
-        GBC_CUDA(cudaGetLastError());
+        if (int rc = ens_theta(e->d_models, e->n, 1, s)) return rc;
         count_launches(1);
     }
-    // a captured group of persistent launches, relaunched until every model reports done
+    // a captured group of persistent launches (one per cluster size, on forked streams), relaunched
+    // until every model reports done
     const int group = 4;
-    if (!e->exec || e->exec_block != e->block) {
-        if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
+    if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
+    {
         cudaGraph_t g;
         GBC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         int rc = 0;
-        for (int k = 0; k < group && !rc; ++k) rc = ens_launch(e, A, e->block, s);
+        for (int k = 0; k < group && !rc; ++k)
+            rc = ens_run_groups(e->lp, o->reltol, o->abstol, o->dtmax, o->dtmin, 250000000ull, e->block, e->smem, s);
         cudaError_t ce = cudaStreamEndCapture(s, &g);
         if (rc) return rc;
         GBC_CUDA(ce);
@@ -638,7 +750,6 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
     }
     for (;;) {
         GBC_CUDA(cudaGraphLaunch(e->exec, s));
-        count_launches(group);
         GBC_CUDA(cudaMemcpyAsync(e->host.data(), e->d_models, sizeof(EnsModel) * e->n, cudaMemcpyDeviceToHost, s));
         GBC_CUDA(cudaStreamSynchronize(s));
         bool all = true;
@@ -646,8 +757,7 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
         if (all) break;
     }
     if (e->log_theta) {
-        k_ens_theta<<<e->n, 256, 0, s>>>(A, 0);
-        GBC_CUDA(cudaGetLastError());
+        if (int rc = ens_theta(e->d_models, e->n, 0, s)) return rc;
         count_launches(1);
     }
     if (u_dev != e->u) GBC_CUDA(cudaMemcpyAsync(u_dev, e->u, sizeof(double) * 3 * e->total_n, cudaMemcpyDeviceToDevice, s));

@@ -28,6 +28,10 @@ struct EnsModel {
 struct EnsArgs {
     EnsModel* models;
     int nmodels;
+    const int* order;            // models of this launch, grouped by cluster size: order[first + i]
+    int first;
+    double* part;                // per model x 16 cluster ranks: error-norm partial sums
+    int* ctl;                    // per model: stop flag of the current step (written by rank 0)
     double reltol, abstol, dtmax, dtmin;
     int budget;                      // step cap per launch and model
     unsigned long long budget_ns;    // wall-clock budget per launch (all models stay busy until done)
@@ -39,9 +43,25 @@ int ens_prepare_model(EnsModel& m, int nx, int nxi, size_t* smem_bytes);
 size_t ens_ghat_floats(const EnsModel& m);
 // real spectra of the model's circulant kernels from its real Toeplitz kernel (device)
 int ens_ghat(const double* st_dev, const EnsModel& m, float* ghat_dev, cudaStream_t s);
-// one persistent launch over n device descriptors, each model runs until done or budget_ns
-int ens_run(EnsModel* d_models, int n, double reltol, double abstol, double dtmax, double dtmin,
-            unsigned long long budget_ns, int block, size_t smem, cudaStream_t s);
+// Models are grouped by cluster size (1, 2, 4 or 8 CTAs per model, from the patch count); each
+// group is one persistent cluster launch on its own stream, forked from and joined to `main`.
+struct EnsLaunch {
+    EnsModel* models = nullptr;
+    int n = 0, cap = 0;
+    const int* order = nullptr;  // device: model indices grouped by cluster size
+    double* part = nullptr;      // device: error-norm partials, 16 per model
+    int* ctl = nullptr;          // device: stop flags, one per model
+    int first[4] = {0, 0, 0, 0}, count[4] = {0, 0, 0, 0};
+    cudaStream_t aux[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+int ens_csize(int N, int maxc);
+int ens_launch_create(EnsLaunch& L, int capacity);
+void ens_launch_destroy(EnsLaunch& L);
+int ens_launch_prepare(EnsLaunch& L, EnsModel* d_models, const EnsModel* host, int n, int maxc, cudaStream_t s);
+// one persistent launch per group: each model runs until done or budget_ns of wall clock
+int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtmax, double dtmin,
+                   unsigned long long budget_ns, int block, size_t smem, cudaStream_t main);
 // θ <-> ln θ on the state of every descriptor with `logged` set
 int ens_theta(EnsModel* d_models, int n, int to_log, cudaStream_t s);
 void count_launches(long long n);

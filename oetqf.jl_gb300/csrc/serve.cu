@@ -70,6 +70,7 @@ struct gbc_server {
     cudaStream_t batch = nullptr, admit = nullptr;
     EnsModel* d_desc = nullptr;
     int d_desc_cap = 0;
+    EnsLaunch lp;
     std::mutex mu;
     std::condition_variable cv;       // new work / stop
     std::condition_variable done_cv;  // request finished
@@ -281,13 +282,15 @@ static void scheduler(gbc_server* s) {
         int rc = 0;
         if (n > s->d_desc_cap) {
             if (s->d_desc) cudaFree(s->d_desc);
+            ens_launch_destroy(s->lp);
             s->d_desc_cap = std::max(n, 2 * s->d_desc_cap);
             if (cudaMalloc(&s->d_desc, sizeof(EnsModel) * s->d_desc_cap) != cudaSuccess) rc = GBC_ENOMEM;
+            if (!rc) rc = ens_launch_create(s->lp, s->d_desc_cap);
         }
         if (!rc && cudaMemcpyAsync(s->d_desc, h.data(), sizeof(EnsModel) * n, cudaMemcpyHostToDevice, s->batch) != cudaSuccess) rc = GBC_ECUDA;
-        if (!rc) rc = ens_run(s->d_desc, n, s->batch_opts.reltol, s->batch_opts.abstol, s->batch_opts.dtmax,
-                              s->batch_opts.dtmin, s->slice_ns, s->block, smem, s->batch);
-        count_launches(1);
+        if (!rc) rc = ens_launch_prepare(s->lp, s->d_desc, h.data(), n, 8, s->batch);
+        if (!rc) rc = ens_run_groups(s->lp, s->batch_opts.reltol, s->batch_opts.abstol, s->batch_opts.dtmax,
+                                     s->batch_opts.dtmin, s->slice_ns, s->block, smem, s->batch);
         if (!rc && cudaMemcpyAsync(h.data(), s->d_desc, sizeof(EnsModel) * n, cudaMemcpyDeviceToHost, s->batch) != cudaSuccess) rc = GBC_ECUDA;
         if (!rc && cudaStreamSynchronize(s->batch) != cudaSuccess) rc = GBC_ECUDA;
         std::vector<std::shared_ptr<Req>> fin;
@@ -416,6 +419,7 @@ void gbc_server_destroy(gbc_server* s) {
     }
     if (s->sched.joinable()) s->sched.join();
     if (s->d_desc) cudaFree(s->d_desc);
+    ens_launch_destroy(s->lp);
     cudaStreamSynchronize(s->batch);
     cudaStreamSynchronize(s->admit);
     cudaStreamDestroy(s->batch);

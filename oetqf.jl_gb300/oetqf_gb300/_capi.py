@@ -78,6 +78,7 @@ def lib():
             "gbc_ensemble_set_fault_props": [P, I, PD, PD, PD, PD, D, D, D, D],
             "gbc_ensemble_set_block": [P, I],
             "gbc_ensemble_set_log_theta": [P, I],
+            "gbc_ensemble_set_max_cluster": [P, I],
             "gbc_ensemble_integrate": [P, PD, PD, PD, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
             "gbc_ensemble_integrate_dev": [P, P, PD, PD, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
         }

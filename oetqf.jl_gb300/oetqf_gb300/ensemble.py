@@ -67,6 +67,9 @@ class Ensemble:
         C.check(C.lib().gbc_ensemble_set_block(self.h, threads))
         self.block = threads
 
+    def set_max_cluster(self, ctas: int):
+        C.check(C.lib().gbc_ensemble_set_max_cluster(self.h, ctas))
+
     def set_log_theta(self, on: bool):
         C.check(C.lib().gbc_ensemble_set_log_theta(self.h, int(bool(on))))
 
@@ -95,13 +98,16 @@ class Ensemble:
             C.check(rc)
         return list(st)
 
-    def autotune(self, u0, t_probe, candidates=(128, 256, 512), **solver):
-        """Times the same short window from u0 with each CTA size and keeps the fastest."""
+    def autotune(self, u0, steps=200, candidates=(128, 256, 512), **solver):
+        """Times the same fixed number of Tsit5 steps for every model (a horizon too long to reach,
+        capped by maxiters) with each CTA size and keeps the fastest: per-step cost, not the mix of
+        cheap and expensive steps in a short time window, decides."""
+        solver = {k: v for k, v in solver.items() if k != "maxiters"}
         timings = {}
         for b in candidates:
             self.set_block(b)
             t0 = time.perf_counter()
-            self.integrate(u0, 0.0, t_probe, **solver)
+            self.integrate(u0, 0.0, 1e15, maxiters=steps, **solver)
             timings[b] = time.perf_counter() - t0
         best = min(timings, key=timings.get)
         self.set_block(best)

@@ -60,3 +60,24 @@ def test_per_model_horizons_and_blocks():
     np.testing.assert_array_equal(outs[128][e.offsets[3]:e.offsets[4]], u0[e.offsets[3]:e.offsets[4]])
     for b in (256, 512):  # CTA size changes reduction order only
         np.testing.assert_allclose(outs[b], outs[128], rtol=1e-6, atol=1e-12)
+
+
+def test_cluster_split_models(oracle):
+    """Models above 600 patches run on 2-8 CTA clusters; they agree with the one-CTA path and with
+    the FP64 oracle."""
+    models = fault_ensemble(n_models=3, n_range=(700, 700), seed=19) + fault_ensemble(n_models=1, n_range=(1300, 1300), seed=23) \
+        + fault_ensemble(n_models=1, n_range=(2500, 2500), seed=29)
+    T = 1 * YEAR
+    e, u0 = _build(models)
+    u8, st8 = e.integrate(u0, 0.0, T, reltol=1e-8, abstol=1e-10, dt=1e-3)
+    e.set_max_cluster(1)
+    u1, st1 = e.integrate(u0, 0.0, T, reltol=1e-8, abstol=1e-10, dt=1e-3)
+    assert all(s.status == 0 for s in st8 + st1)
+    np.testing.assert_allclose(u8, u1, rtol=1e-7, atol=1e-15)  # error-norm reduction order differs
+    for i in (0, 3):
+        m = models[i]
+        gf = oracle.gf_ff(m.mf, m.lam, m.mu, fourier=True)
+        uc, _ = oracle.OracleModel(gf, m.pf).integrate(m.u0, 0.0, T, reltol=1e-8, abstol=1e-10, dt0=1e-3)
+        N = m.N
+        ui = u8[e.offsets[i]:e.offsets[i] + 3 * N]
+        assert np.abs(ui[:N] - uc[:N]).max() / np.abs(uc[:N]).max() < 1e-4
