@@ -246,7 +246,9 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
                 for (int s = 0; s < 7; ++s) e = fma(e_te[s], kk[s][g], e);
                 e *= dt;
                 const double unv = un[g];
-                const double sc = A.abstol + A.reltol * fmax(fabs(u[g]), fabs(unv));
+                // ψ = ln θ: an absolute ψ error is a relative θ error, scaled by reltol
+                const double sc = (comp == 1 && m.log_theta) ? A.abstol + A.reltol
+                                                             : A.abstol + A.reltol * fmax(fabs(u[g]), fabs(unv));
                 const double r = e / sc;
                 ss = fma(r, r, ss);
                 bad |= !isfinite(unv);
@@ -384,9 +386,12 @@ int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtma
         cudaStream_t s = L.aux[g];
         GBC_CUDA(cudaStreamWaitEvent(s, L.fork, 0));
         A.first = L.first[g];
+        // models split over clusters are the large ones: 512 threads per CTA measured best for them;
+        // the one-CTA group uses the (autotuned) block size
+        const int b = (g > 0) ? 512 : block;
         int rc;
-        if (block == 128) rc = launch_cluster<128>(A, L.count[g], 1 << g, smem, s);
-        else if (block == 512) rc = launch_cluster<512>(A, L.count[g], 1 << g, smem, s);
+        if (b == 128) rc = launch_cluster<128>(A, L.count[g], 1 << g, smem, s);
+        else if (b == 512) rc = launch_cluster<512>(A, L.count[g], 1 << g, smem, s);
         else rc = launch_cluster<256>(A, L.count[g], 1 << g, smem, s);
         if (rc) return rc;
         GBC_CUDA(cudaEventRecord(L.join[g], s));

@@ -56,7 +56,9 @@ __global__ void k_error_control(long long n, const double* __restrict__ u, const
         for (int s = 0; s < 7; ++s) e = fma(c_te[s], K.k[s][i], e);
         e *= dt;
         const double unv = un[i];
-        const double sc = atol + rtol * fmax(fabs(u[i]), fabs(unv));
+        // with ψ = ln θ an absolute ψ error equals a relative θ error: scale it by reltol
+        const double sc = (c->log_theta && i >= c->th_lo && i < c->th_hi) ? atol + rtol
+                                                                             : atol + rtol * fmax(fabs(u[i]), fabs(unv));
         const double r = e / sc;
         ss = fma(r, r, ss);
         bad |= !isfinite(unv);
@@ -185,6 +187,9 @@ int integrator_run(Integrator& I, const RhsArgs& rhs0, double* u, double t0, dou
                    double abstol, double dt0, double dtmax, double dtmin, long long maxiters,
                    cudaStream_t s) {
     Ctrl h{};
+    h.log_theta = rhs0.log_theta;
+    h.th_lo = rhs0.N;
+    h.th_hi = 2LL * rhs0.N;
     h.t = t0;
     h.t1 = t1;
     h.dt = std::min(dt0, dtmax);

@@ -11,8 +11,9 @@ struct Ctrl {
     double t, dt, t1, qold;
     double reltol, abstol, dtmax, dtmin;
     long long naccept, nreject, nrhs, iters, maxiters;
-    int done, status, accept, pad;
+    int done, status, accept, log_theta;
     unsigned int blocks_done;
+    long long th_lo, th_hi;  // θ slot of the state; holds ψ = ln θ when log_theta
 };
 
 struct Integrator {
