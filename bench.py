@@ -197,6 +197,8 @@ def run_gpu(args):
     stream = torch.cuda.ExternalStream(m.stream)
     u = torch.tensor(cm.u0, device="cuda")
     if args.profile_rhs:
+        if args.profile_precision != "f64":
+            m.set_precision(C.GBC_PREC_BF16 if args.profile_precision == "bf16" else C.GBC_PREC_F16)
         du = torch.zeros_like(u)
         for _ in range(args.profile_rhs):
             m.rhs_dev(u.data_ptr(), du.data_ptr())
@@ -444,6 +446,22 @@ def run_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
+def run_ensemble_profile(args):
+    """Short ensemble run for ncu captures of the persistent kernel (0.01 yr of the 256 models)."""
+    from oetqf_gb300.ensemble import Ensemble
+    models = fault_ensemble(n_models=256, years=0.01)
+    e = Ensemble([(mm.mf.nx, mm.mf.nξ) for mm in models])
+    for i, mm in enumerate(models):
+        e.assemble(i, mm.mf, mm.lam, mm.mu)
+        e.set_fault_props(i, mm.pf)
+    u0 = np.zeros(e.state_len)
+    for i, mm in enumerate(models):
+        u0[e.offsets[i]:e.offsets[i] + mm.u0.size] = mm.u0
+    e.set_block(256)
+    u, st = e.integrate(u0, 0.0, 0.01 * YEAR, **SOLVER)
+    print(json.dumps({"profile_ensemble": True, "steps": int(sum(s.naccept + s.nreject for s in st))}))
+
+
 def run_serving(args):
     from oetqf_gb300.serving import Server, run_stream
     reqs = serving_requests(n_requests=args.requests)
@@ -469,7 +487,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbcycle", choices=["gbcycle", "reference"])
     ap.add_argument("--workload", default="fault-mantle-1000x2500-f64",
-                    choices=list(STEPS_FOR_HORIZON) + ["fault-mantle-4096x8000-mixed", "ensemble-256", "serving"])
+                    choices=list(STEPS_FOR_HORIZON) + ["fault-mantle-4096x8000-mixed", "ensemble-256", "serving",
+                                                       "ensemble-profile"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "f16"])
     ap.add_argument("--fp64-sample", type=int, default=8)
     ap.add_argument("--requests", type=int, default=32)
@@ -478,6 +497,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-rhs", type=int, default=0, help="run N right-hand sides only (for ncu captures)")
     ap.add_argument("--years", type=float, default=0.0, help="override the horizon (profiling runs only)")
+    ap.add_argument("--profile-precision", default="f64", choices=["f64", "bf16", "f16"])
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -485,6 +505,8 @@ def main():
         run_mixed_large(args)
     elif args.workload == "ensemble-256":
         run_ensemble(args)
+    elif args.workload == "ensemble-profile":
+        run_ensemble_profile(args)
     elif args.workload == "serving":
         run_serving(args)
     else:
