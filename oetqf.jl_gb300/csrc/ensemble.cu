@@ -50,24 +50,54 @@ struct EnsSmem {
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 
-// in-place radix-2 DIT FFT of nq arrays of length P already in bit-reversed order; sign -1
-// forward (twiddles e^{-2πi t/P}), +1 inverse (conjugated twiddles, no scaling)
+// in-place radix-2 DIT FFT of nq arrays of length P already in bit-reversed order; forward uses
+// twiddles e^{-2πi t/P}, inverse their conjugates (no scaling). Two consecutive radix-2 stages are
+// done per pass with a thread's four elements in registers (the same operations in the same
+// order), so a pass needs one barrier instead of two.
 template <int BS>
 __device__ __forceinline__ void fft_many(float2* Z, int nq, int P, int logP, const float2* tw, int inverse) {
-    const int half_total = P >> 1;
-    for (int st = 0; st < logP; ++st) {
-        const int half = 1 << st;
-        const int tstride = P >> (st + 1);
-        for (int t = threadIdx.x; t < nq * half_total; t += BS) {
-            const int q = t / half_total, b = t - q * half_total;
-            const int grp = b >> st, pos = b & (half - 1);
-            const int i0 = (grp << (st + 1)) + pos, i1 = i0 + half;
-            float2 w = tw[pos * tstride];
-            if (inverse) w.y = -w.y;
-            float2* z = Z + q * P;
-            const float2 a = z[i0], c = cmul(z[i1], w);
-            z[i0] = make_float2(a.x + c.x, a.y + c.y);
-            z[i1] = make_float2(a.x - c.x, a.y - c.y);
+    int st = 0;
+    while (st < logP) {
+        if (st + 1 < logP) {
+            const int h = 1 << st;
+            const int quarter = P >> 2;
+            const int s1 = P / (2 * h), s2 = P / (4 * h);
+            for (int t = threadIdx.x; t < nq * quarter; t += BS) {
+                const int q = t / quarter, r = t - q * quarter;
+                const int g = r >> st, pos = r & (h - 1);
+                const int b0 = g * 4 * h + pos;
+                float2* z = Z + q * P;
+                float2 w1 = tw[pos * s1], w2a = tw[pos * s2], w2b = tw[(pos + h) * s2];
+                if (inverse) { w1.y = -w1.y; w2a.y = -w2a.y; w2b.y = -w2b.y; }
+                float2 x0 = z[b0], x1 = z[b0 + h], x2 = z[b0 + 2 * h], x3 = z[b0 + 3 * h];
+                float2 c = cmul(x1, w1);
+                float2 y0 = make_float2(x0.x + c.x, x0.y + c.y), y1 = make_float2(x0.x - c.x, x0.y - c.y);
+                c = cmul(x3, w1);
+                float2 y2 = make_float2(x2.x + c.x, x2.y + c.y), y3 = make_float2(x2.x - c.x, x2.y - c.y);
+                c = cmul(y2, w2a);
+                z[b0] = make_float2(y0.x + c.x, y0.y + c.y);
+                z[b0 + 2 * h] = make_float2(y0.x - c.x, y0.y - c.y);
+                c = cmul(y3, w2b);
+                z[b0 + h] = make_float2(y1.x + c.x, y1.y + c.y);
+                z[b0 + 3 * h] = make_float2(y1.x - c.x, y1.y - c.y);
+            }
+            st += 2;
+        } else {
+            const int half = 1 << st;
+            const int half_total = P >> 1;
+            const int tstride = P >> (st + 1);
+            for (int t = threadIdx.x; t < nq * half_total; t += BS) {
+                const int q = t / half_total, b = t - q * half_total;
+                const int grp = b >> st, pos = b & (half - 1);
+                const int i0 = (grp << (st + 1)) + pos, i1 = i0 + half;
+                float2 w = tw[pos * tstride];
+                if (inverse) w.y = -w.y;
+                float2* z = Z + q * P;
+                const float2 a = z[i0], c = cmul(z[i1], w);
+                z[i0] = make_float2(a.x + c.x, a.y + c.y);
+                z[i1] = make_float2(a.x - c.x, a.y - c.y);
+            }
+            st += 1;
         }
         __syncthreads();
     }
