@@ -90,6 +90,15 @@ int gbc_model_set_fault_props(gbc_model* m, const double* a, const double* b, co
  * deps0 of length 6 (xx, xy, xz, yy, yz, zz). */
 int gbc_model_set_mantle_props(gbc_model* m, const double* gamma, const double* n,
                                const double* deps0);
+/* CompositePowerLawViscosityProperty (src/BEM/property.jl:43-48, equation.jl:286-292): nlaws
+ * power laws summed; gamma and n are (ne, nlaws) column-major (law k at offset k*ne). */
+int gbc_model_set_mantle_props_composite(gbc_model* m, int nlaws, const double* gamma,
+                                         const double* n, const double* deps0);
+/* DilatancyProperty (src/BEM/property.jl:27-32) for a fault-only model: the ode becomes
+ * equation.jl:168-183 with update_fault_with_dilatancy! (:248-276) and d𝓅_dt (:282); the state is
+ * (v, θ, δ, 𝓅), four (nx,nxi) parts. tp, eps, beta, p0 are (nx,nxi). FP64 path. */
+int gbc_model_set_dilatancy(gbc_model* m, const double* tp, const double* eps, const double* beta,
+                            const double* p0);
 
 #define GBC_GF11_REAL 0   /* (nx,nxi,nxi) real Toeplitz kernel */
 #define GBC_GF11_DFT 1    /* (nx,nxi,nxi) complex interleaved, the reference's fourier=true form */
@@ -118,8 +127,9 @@ int gbc_model_set_log_theta(gbc_model* m, int on);
  * timed out and the last right-hand side is not valid. */
 int gbc_model_error_word(gbc_model* m);
 
-/* ode(du, u, p, t) (equation.jl:156-166 / 185-205) on host buffers in ArrayPartition order:
- * nparts = 3: (v, θ, δ), each (nx,nxi); nparts = 5: (v, θ, ϵ, σ, δ), ϵ and σ (ne,6). */
+/* ode(du, u, p, t) (equation.jl:156-166 / 168-183 / 185-205) on host buffers in ArrayPartition
+ * order: nparts = 3: (v, θ, δ), each (nx,nxi); 4 with dilatancy: (v, θ, δ, 𝓅);
+ * 5: (v, θ, ϵ, σ, δ), ϵ and σ (ne,6). */
 int gbc_rhs(gbc_model* m, double t, const double* const* u_parts, double* const* du_parts,
             int nparts);
 /* Same on device memory: u and du are the flat concatenation of the parts (length

@@ -148,7 +148,9 @@ struct gbc_model {
     long long M = 0;
     size_t ldm = 0, ld21 = 0;
     cudaStream_t stream = nullptr;
-    DevBuf st, gm, g21, a, b, L, sig, gamma, nexp, xm, u, du;
+    DevBuf st, gm, g21, a, b, L, sig, gamma, nexp, xm, u, du, tp, deps_d, beta_d, p0;
+    int nlaws = 1;
+    int dila = 0;
     double eta = 0, vpl = 0, f0 = 0.6, v0 = 1e-6, deps0[6] = {0, 0, 0, 0, 0, 0};
     bool props = false, mprops = false, has_st = false, has_g12 = false, has_g21 = false, has_g22 = false;
     int precision = GBC_PREC_F64;
@@ -166,8 +168,10 @@ struct gbc_model {
         r.st = st.p; r.gm = gm.p; r.ldm = ldm; r.g21 = g21.p; r.ld21 = ld21;
         r.a = a.p; r.b = b.p; r.L = L.p; r.sig = sig.p;
         r.eta = eta; r.vpl = vpl; r.f0 = f0; r.v0 = v0;
-        r.gamma = gamma.p; r.nexp = nexp.p;
+        r.gamma = gamma.p; r.nexp = nexp.p; r.nlaws = nlaws;
         for (int k = 0; k < 6; ++k) r.deps0[k] = deps0[k];
+        r.dila = dila;
+        r.tp = tp.p; r.deps_d = deps_d.p; r.beta_d = beta_d.p; r.p0 = p0.p;
         r.xm = xm.p;
         r.skip = nullptr;
         r.log_theta = 0;
@@ -217,7 +221,7 @@ struct gbc_model {
             return fail(GBC_ESTATE, "viscoelastic model needs mantle properties and gf12, gf21, gf22");
         return 0;
     }
-    long long state_len() const { return layout_of(N, ne).n; }
+    long long state_len() const { return layout_of(N, ne, dila).n; }
 };
 
 extern "C" {
@@ -445,14 +449,36 @@ int gbc_model_set_fault_props(gbc_model* m, const double* a, const double* b, co
 }
 
 int gbc_model_set_mantle_props(gbc_model* m, const double* gamma, const double* n, const double* deps0) {
+    return gbc_model_set_mantle_props_composite(m, 1, gamma, n, deps0);
+}
+
+int gbc_model_set_mantle_props_composite(gbc_model* m, int nlaws, const double* gamma, const double* n,
+                                         const double* deps0) {
     if (!m || !gamma || !n || !deps0) return fail(GBC_EINVAL, "null argument");
     if (m->ne == 0) return fail(GBC_EINVAL, "fault-only model has no mantle");
+    if (nlaws < 1) return fail(GBC_EINVAL, "a composite viscosity needs at least one law");
     cudaStream_t s = m->stream;
-    if (int rc = upload(m->gamma, gamma, m->ne, s)) return rc;
-    if (int rc = upload(m->nexp, n, m->ne, s)) return rc;
+    if (int rc = upload(m->gamma, gamma, (size_t)nlaws * m->ne, s)) return rc;
+    if (int rc = upload(m->nexp, n, (size_t)nlaws * m->ne, s)) return rc;
     GBC_CUDA(cudaStreamSynchronize(s));
     for (int k = 0; k < 6; ++k) m->deps0[k] = deps0[k];
+    m->nlaws = nlaws;
     m->mprops = true;
+    return 0;
+}
+
+int gbc_model_set_dilatancy(gbc_model* m, const double* tp, const double* eps, const double* beta, const double* p0) {
+    if (!m || !tp || !eps || !beta || !p0) return fail(GBC_EINVAL, "null argument");
+    if (m->ne != 0) return fail(GBC_EINVAL, "dilatancy applies to fault-only models (equation.jl:168-183)");
+    cudaStream_t s = m->stream;
+    if (int rc = upload(m->tp, tp, m->N, s)) return rc;
+    if (int rc = upload(m->deps_d, eps, m->N, s)) return rc;
+    if (int rc = upload(m->beta_d, beta, m->N, s)) return rc;
+    if (int rc = upload(m->p0, p0, m->N, s)) return rc;
+    m->dila = 1;
+    if (int rc = m->u.alloc((size_t)m->state_len())) return rc;
+    if (int rc = m->du.alloc((size_t)m->state_len())) return rc;
+    GBC_CUDA(cudaStreamSynchronize(s));
     return 0;
 }
 
@@ -598,12 +624,12 @@ int gbc_rhs_dev(gbc_model* m, double t, const double* u, double* du) {
 
 int gbc_rhs(gbc_model* m, double t, const double* const* u_parts, double* const* du_parts, int nparts) {
     if (!m || !u_parts || !du_parts) return fail(GBC_EINVAL, "null argument");
-    const int want = m->ne > 0 ? 5 : 3;
+    const int want = m->ne > 0 ? 5 : (m->dila ? 4 : 3);
     if (nparts != want) return fail(GBC_EINVAL, "ArrayPartition must have " + std::to_string(want) + " components");
     if (int rc = m->ready()) return rc;
     if (int rc = m->prepare()) return rc;
     const long long N = m->N, E = m->M;
-    long long len[5] = {N, N, N, 0, 0};
+    long long len[5] = {N, N, N, N, 0};
     if (want == 5) { len[2] = E; len[3] = E; len[4] = N; }
     cudaStream_t s = m->stream;
     long long off = 0;
@@ -644,13 +670,13 @@ static int integrate_common(gbc_model* m, double* u_dev, double t0, double t1, c
     if (int rc = m->prepare()) return rc;
     if (int rc = integrator_alloc(m->integ, m->state_len())) return rc;
     RhsArgs args = m->args();
-    args.log_theta = m->log_theta;
-    if (m->log_theta) {
+    args.log_theta = m->dila ? 0 : m->log_theta;
+    if (args.log_theta) {
         if (int rc = theta_transform(u_dev + m->N, m->N, 1, m->stream)) return rc;
     }
     int rc = integrator_run(m->integ, args, u_dev, t0, t1, o->reltol, o->abstol, o->dt0, o->dtmax,
                             o->dtmin, o->maxiters, m->stream);
-    if (m->log_theta) {
+    if (args.log_theta) {
         if (int rc2 = theta_transform(u_dev + m->N, m->N, 0, m->stream)) return rc2;
     }
     const Ctrl& c = *m->integ.ctrl_host;

@@ -292,7 +292,8 @@ __global__ void k_prologue_mixed(RhsArgs a, const double* __restrict__ u, double
         const double sxx = s[i] - skk, syy = s[i + 3 * ne] - skk, szz = s[i + 5 * ne] - skk;
         const double sxy = s[i + ne], sxz = s[i + 2 * ne], syz = s[i + 4 * ne];
         const double tau = sqrt(sxx * sxx + syy * syy + szz * szz + 2.0 * (sxy * sxy + sxz * sxz + syz * syz));
-        const double f = a.gamma[i] * pow(tau, a.nexp[i]);
+        double f = 0.0;
+        for (int q = 0; q < a.nlaws; ++q) f += a.gamma[i + (size_t)q * ne] * pow(tau, a.nexp[i + (size_t)q * ne]);
         const double d[6] = {f * sxx, f * sxy, f * sxz, f * syy, f * syz, f * szz};
         double* deps = du + L.eps;
 #pragma unroll

@@ -72,7 +72,7 @@ extern "C" int gbc_rhs_visco_noalloc(int nx, int nxi, int ne, const double* st, 
     r.st = st; r.gm = gm; r.ldm = ldm; r.g21 = g21; r.ld21 = ld21;
     r.a = a; r.b = b; r.L = L; r.sig = sigma;
     r.eta = eta; r.vpl = vpl; r.f0 = f0; r.v0 = v0;
-    r.gamma = gamma; r.nexp = n;
+    r.gamma = gamma; r.nexp = n; r.nlaws = 1;
     for (int k = 0; k < 6; ++k) r.deps0[k] = deps0[k];  // host array, passed by value to the kernels
     r.xm = x;
     r.skip = nullptr;

@@ -19,9 +19,13 @@ struct RhsArgs {
     // friction (property.jl:10-25)
     const double *a, *b, *L, *sig;
     double eta, vpl, f0, v0;
-    // viscosity (property.jl:34-41)
+    // viscosity (property.jl:34-48): nlaws power laws summed, gamma/nexp are (nlaws x ne) law-major
     const double *gamma, *nexp;
+    int nlaws;
     double deps0[6];
+    // dilatancy (property.jl:27-32): nonzero -> fault-only state (v, θ, δ, 𝓅)
+    int dila;
+    const double *tp, *deps_d, *beta_d, *p0;
     // scratch: x = [v - vpl (N); 0 (npad - N); dϵ - dϵ₀ (6ne)]
     double* xm;
     // optional device flag: when non-null and nonzero the launch does nothing (finished solve)
@@ -42,13 +46,21 @@ struct RhsArgs {
 
 // state offsets in the flat ArrayPartition layout
 struct StateLayout {
-    long long v, th, eps, sig, delta, n;
+    long long v, th, eps, sig, delta, p, n;
 };
-inline StateLayout layout_of(int N, int ne) {
+inline StateLayout layout_of(int N, int ne, int dila = 0) {
     StateLayout s;
     const long long E = 6LL * ne;
     s.v = 0;
     s.th = N;
+    s.p = -1;
+    if (dila) {  // (v, θ, δ, 𝓅), equation.jl:176-177
+        s.eps = s.sig = -1;
+        s.delta = 2LL * N;
+        s.p = 3LL * N;
+        s.n = 4LL * N;
+        return s;
+    }
     if (ne > 0) {
         s.eps = 2LL * N;
         s.sig = 2LL * N + E;

@@ -65,7 +65,8 @@ __global__ void k_prologue(RhsArgs a, const double* __restrict__ u, double* __re
         const double sxx = s[i] - skk, syy = s[i + 3 * ne] - skk, szz = s[i + 5 * ne] - skk;
         const double sxy = s[i + ne], sxz = s[i + 2 * ne], syz = s[i + 4 * ne];
         const double tau = sqrt(sxx * sxx + syy * syy + szz * szz + 2.0 * (sxy * sxy + sxz * sxz + syz * syz));
-        const double f = a.gamma[i] * pow(tau, a.nexp[i]);
+        double f = 0.0;  // equation.jl:285 (one law) or :286-292 (composite: sum of laws)
+        for (int q = 0; q < a.nlaws; ++q) f += a.gamma[i + (size_t)q * ne] * pow(tau, a.nexp[i + (size_t)q * ne]);
         const double d[6] = {f * sxx, f * sxy, f * sxz, f * syy, f * syz, f * szz};
         double* deps = du + L.eps;
 #pragma unroll
@@ -103,7 +104,22 @@ __global__ void __launch_bounds__(256) k_rows(RhsArgs a, const double* __restric
         }
         if (M > 0) acc += warp_dot(a.g21 + (size_t)i * a.ld21, a.xm + a.npad, M, lane);
         const double dtau = warp_sum(acc);
-        if (lane == 0) {
+        if (lane == 0 && a.dila) {
+            // update_fault_with_dilatancy! (equation.jl:248-276) and d𝓅_dt (:282)
+            const double vi = v[i], th = u[L.th + i], pi = u[L.p + i];
+            const double Li = a.L[i];
+            const double dth = 1.0 - vi * th / Li;
+            const double dp = -(pi - a.p0[i]) / a.tp[i] + a.deps_d[i] / a.beta_d[i] / th * dth;
+            const double af = a.a[i] / a.f0, bf = a.b[i] / a.f0;
+            const double vf = fmax(0.0, vi / a.v0), thf = fmax(0.0, th * a.v0 / Li);
+            const double vfa1 = pow(vf, af - 1.0), thfb1 = pow(thf, bf - 1.0);
+            const double vfa = pow(vf, af), thfb = pow(thf, bf);
+            du[L.th + i] = dth;
+            du[L.p + i] = dp;
+            du[L.v + i] = (dtau + a.f0 * dp * vfa * thfb - a.f0 * (a.sig[i] - pi) * vfa * thfb1 * bf * a.v0 / Li * dth) /
+                          (a.f0 * (a.sig[i] - pi) * vfa1 * thfb * af / a.v0);
+            du[L.delta + i] = vi;
+        } else if (lane == 0) {
             const double vi = v[i], th = a.log_theta ? exp(u[L.th + i]) : u[L.th + i];
             const double ai = a.a[i], bi = a.b[i], Li = a.L[i];
             const double psi1 = exp((a.f0 + bi * log(a.v0 * fmax(0.0, th) / Li)) / ai) / (2.0 * a.v0);
@@ -119,13 +135,13 @@ __global__ void __launch_bounds__(256) k_rows(RhsArgs a, const double* __restric
 }
 
 int rhs_kernel_count(const RhsArgs& a) {
-    if (a.mode != 0) return a.ne > 0 ? 3 : 1;
+    if (a.mode != 0 && !a.dila) return a.ne > 0 ? 3 : 1;
     return a.ne > 0 ? 2 : 1;
 }
 
 int launch_rhs(const RhsArgs& a, const double* u, double* du, cudaStream_t s) {
-    if (a.mode != 0) return launch_rhs_mixed(a, u, du, s);
-    const StateLayout L = layout_of(a.N, a.ne);
+    if (a.mode != 0 && !a.dila) return launch_rhs_mixed(a, u, du, s);
+    const StateLayout L = layout_of(a.N, a.ne, a.dila);
     const int sms = sm_count();
     if (a.ne > 0) {
         const int n = a.N + a.ne;

@@ -6,11 +6,17 @@ side (src/BEM/equation.jl), and an on-device adaptive integrator. Compute runs i
 """
 from .mesh import (BEMHex8Mesh, RectOkadaMesh, gauss1_quadrature, gauss_product_quadrature, gen_hex8_box,
                    gen_mesh, sincosd)
-from .property import PowerLawViscosityProperty, RateStateQuasiDynamicProperty, dϵ_dt
+from .property import (CompositePowerLawViscosityProperty, DilatancyProperty, PowerLawViscosityProperty,
+                       RateStateQuasiDynamicProperty, dϵ_dt, dϵ_dt_composite)
+
+import unicodedata as _ud
 
 __all__ = ["BEMHex8Mesh", "RectOkadaMesh", "gen_mesh", "gen_hex8_box", "gauss1_quadrature", "gauss_product_quadrature",
-           "sincosd", "RateStateQuasiDynamicProperty", "PowerLawViscosityProperty", "dϵ_dt", "stress_greens_function",
+           "sincosd", "RateStateQuasiDynamicProperty", "PowerLawViscosityProperty", "CompositePowerLawViscosityProperty",
+           "DilatancyProperty", "dϵ_dt", "dϵ_dt_composite", "stress_greens_function",
            "StrikeSlip", "DipSlip", "assemble", "solve", "ArrayPartition", "GB300Model", "ODEProblem"]
+# identifiers are NFKC-normalised (ϵ -> ε); keep the exported names in that form
+__all__ = [_ud.normalize("NFKC", n) for n in __all__]
 
 
 def __getattr__(name):

@@ -61,6 +61,8 @@ def lib():
             "gbc_model_create": [I, I, I, ctypes.POINTER(P)],
             "gbc_model_set_fault_props": [P, PD, PD, PD, PD, D, D, D, D],
             "gbc_model_set_mantle_props": [P, PD, PD, PD],
+            "gbc_model_set_mantle_props_composite": [P, I, PD, PD, PD],
+            "gbc_model_set_dilatancy": [P, PD, PD, PD, PD],
             "gbc_model_set_gf": [P, I, PD],
             "gbc_model_assemble": [P, ctypes.POINTER(FaultMesh), ctypes.POINTER(HexMesh), D, D, I, I, D, PD, PD, I],
             "gbc_model_export_gf": [P, I, PD],

@@ -48,6 +48,7 @@ class GB300Model:
     def __init__(self, nx: int, nξ: int, ne: int = 0):
         self.nx, self.nξ, self.ne = nx, nξ, ne
         self.N = nx * nξ
+        self.dilatancy = False
         h = ctypes.c_void_p()
         C.check(C.lib().gbc_model_create(nx, nξ, ne, ctypes.byref(h)))
         self.h = h
@@ -77,9 +78,20 @@ class GB300Model:
         C.check(C.lib().gbc_model_set_fault_props(self.h, k(_fcol(p.a)), k(_fcol(p.b)), k(_fcol(p.L)), k(_fcol(p.σ)),
                                                   float(p.η), float(p.vpl), float(p.f0), float(p.v0)))
 
-    def set_mantle_props(self, p: PowerLawViscosityProperty):
+    def set_mantle_props(self, p):
+        """PowerLawViscosityProperty or CompositePowerLawViscosityProperty."""
         k = C.Keep()
+        if hasattr(p, "piter"):
+            gam = np.concatenate([np.asarray(q.γ, dtype=np.float64) for q in p.piter])
+            nn = np.concatenate([np.asarray(q.n, dtype=np.float64) for q in p.piter])
+            C.check(C.lib().gbc_model_set_mantle_props_composite(self.h, len(p.piter), k(gam), k(nn), k(p.dϵ0)))
+            return
         C.check(C.lib().gbc_model_set_mantle_props(self.h, k(p.γ), k(p.n), k(p.dϵ0)))
+
+    def set_dilatancy(self, d):
+        k = C.Keep()
+        C.check(C.lib().gbc_model_set_dilatancy(self.h, k(_fcol(d.tp)), k(_fcol(d.ϵ)), k(_fcol(d.β)), k(_fcol(d.p0))))
+        self.dilatancy = True
 
     def set_gf(self, which: int, gf):
         g = np.asarray(gf)
@@ -137,7 +149,7 @@ class GB300Model:
     def rhs_flat(self, u: np.ndarray, t: float = 0.0) -> np.ndarray:
         """du for a flat host state (ArrayPartition order)."""
         N, E = self.N, 6 * self.ne
-        sizes = [N, N, N] if self.ne == 0 else [N, N, E, E, N]
+        sizes = ([N, N, N, N] if self.dilatancy else [N, N, N]) if self.ne == 0 else [N, N, E, E, N]
         u = np.ascontiguousarray(u, dtype=np.float64)
         parts = np.split(u, np.cumsum(sizes)[:-1])
         parts = [np.ascontiguousarray(p) for p in parts]
@@ -187,7 +199,16 @@ def _gpu_ode(du, u, p: GB300Model, t):
 
 
 def assemble(*args, **kwargs) -> ODEProblem:
-    """assemble(gf, p, u0, tspan) or assemble(gf₁₁, gf₁₂, gf₂₁, gf₂₂, pf, pa, u0, tspan)."""
+    """assemble(gf, p, u0, tspan), assemble(gf, p, dila, u0, tspan) (equation.jl:108-117) or
+    assemble(gf₁₁, gf₁₂, gf₂₁, gf₂₂, pf, pa, u0, tspan)."""
+    if len(args) == 5:
+        gf, p, dila, u0, tspan = args
+        nx, nξ = np.asarray(u0.x[0]).shape
+        m = GB300Model(nx, nξ, 0)
+        m.set_gf(C.GBC_GF11_DFT if np.iscomplexobj(gf) else C.GBC_GF11_REAL, gf)
+        m.set_fault_props(p)
+        m.set_dilatancy(dila)
+        return ODEProblem(_gpu_ode, u0, tuple(tspan), m)
     if len(args) == 4:
         gf, p, u0, tspan = args
         nx, nξ = np.asarray(u0.x[0]).shape

@@ -69,8 +69,10 @@ typedef struct {
     int nx, nxi, ne;
     const double *a, *b, *L, *sigma;      /* N each */
     double eta, vpl, f0, v0;
-    const double *gamma, *n;              /* ne each (viscous) */
+    const double *gamma, *n;              /* ne each (viscous); nlaws x ne when nlaws > 1 */
+    int nlaws;                            /* CompositePowerLawViscosityProperty: number of laws (0/1 = one) */
     double deps0[6];
+    const double *tp, *deps, *beta, *p0;  /* DilatancyProperty (N each); NULL unless dilatancy */
     const double *gf11_dft;               /* complex interleaved (nx,nxi,nxi) */
     const double *gf12, *gf21, *gf22;     /* (6ne,N), (N,6ne), (6ne,6ne) col-major; NULL if ne=0 */
 } orc_model;
@@ -93,12 +95,17 @@ void orc_ode_fault(const orc_model* m, const double* v, const double* th, double
 void orc_ode_visco(const orc_model* m, const double* v, const double* th, const double* sig,
                    double* dv, double* dth, double* deps, double* dsig, double* ddelta);
 
+/* Fault-only ode with dilatancy (equation.jl:168-183, :248-276, :282):
+ * u = (v, θ, δ, 𝓅), du likewise; each N. */
+void orc_ode_dilatancy(const orc_model* m, const double* v, const double* th, const double* p,
+                       double* dv, double* dth, double* ddelta, double* dp);
+
 /* Adaptive Tsit5 integration of the flattened state in ArrayPartition order.
  * Returns 0 on reaching t1, else a negative status; fills counters. */
 typedef struct {
     double reltol, abstol, dt0, dtmax, dtmin;
     long long maxiters;
-    int mantle;                            /* 0: fault-only state, 1: viscoelastic state */
+    int mantle;                            /* 0: fault-only, 1: viscoelastic, 2: dilatancy state */
 } orc_solver_opts;
 typedef struct { long long naccept, nreject, nrhs; double t, dt; int status; } orc_solver_stats;
 int orc_integrate(const orc_model* m, double* u, double t0, double t1, const orc_solver_opts* o,

@@ -124,7 +124,10 @@ void orc_ode_visco(const orc_model* m, const double* v, const double* th, const 
         double sxx = s[i] - skk, syy = s[i + 3 * ne] - skk, szz = s[i + 5 * ne] - skk;
         double sxy = s[i + ne], sxz = s[i + 2 * ne], syz = s[i + 4 * ne];
         double tau = sqrt(sxx * sxx + syy * syy + szz * szz + 2.0 * (sxy * sxy + sxz * sxz + syz * syz));
-        double f = m->gamma[i] * pow(tau, m->n[i]);
+        /* one law (equation.jl:285) or the sum of a composite's laws (equation.jl:286-292) */
+        double f = 0.0;
+        const int K = m->nlaws > 1 ? m->nlaws : 1;
+        for (int k = 0; k < K; ++k) f += m->gamma[i + (size_t)k * ne] * pow(tau, m->n[i + (size_t)k * ne]);
         deps[i] = f * sxx;
         deps[i + ne] = f * sxy;
         deps[i + 2 * ne] = f * sxz;
@@ -143,13 +146,39 @@ void orc_ode_visco(const orc_model* m, const double* v, const double* th, const 
     free(dtau); free(relv); free(reldeps);
 }
 
+/* update_fault_with_dilatancy! (equation.jl:248-276) with d𝓅_dt (:282) */
+void orc_ode_dilatancy(const orc_model* m, const double* v, const double* th, const double* p,
+                       double* dv, double* dth, double* ddelta, double* dp) {
+    const int N = m->nx * m->nxi;
+    double* dtau = (double*)malloc(sizeof(double) * N);
+    orc_dtau_dt(m, v, dtau);
+    for (int i = 0; i < N; ++i) {
+        dth[i] = 1.0 - v[i] * th[i] / m->L[i];
+        dp[i] = -(p[i] - m->p0[i]) / m->tp[i] + m->deps[i] / m->beta[i] / th[i] * dth[i];
+        const double af = m->a[i] / m->f0, bf = m->b[i] / m->f0;
+        const double vf = fmax(0.0, v[i] / m->v0), thf = fmax(0.0, th[i] * m->v0 / m->L[i]);
+        const double vfa1 = pow(vf, af - 1.0), thfb1 = pow(thf, bf - 1.0);
+        const double vfa = pow(vf, af), thfb = pow(thf, bf);
+        dv[i] = (dtau[i] + m->f0 * dp[i] * vfa * thfb -
+                 m->f0 * (m->sigma[i] - p[i]) * vfa * thfb1 * bf * m->v0 / m->L[i] * dth[i]) /
+                (m->f0 * (m->sigma[i] - p[i]) * vfa1 * thfb * af / m->v0);
+        ddelta[i] = v[i];
+    }
+    free(dtau);
+}
+
 long long orc_state_len(const orc_model* m, int mantle) {
     long long N = (long long)m->nx * m->nxi;
+    if (mantle == 2) return 4 * N;
     return mantle ? 3 * N + 12LL * m->ne : 3 * N;
 }
 
 static void rhs_flat(const orc_model* m, int mantle, const double* u, double* du) {
     const long long N = (long long)m->nx * m->nxi;
+    if (mantle == 2) {
+        orc_ode_dilatancy(m, u, u + N, u + 3 * N, du, du + N, du + 2 * N, du + 3 * N);
+        return;
+    }
     if (!mantle) {
         orc_ode_fault(m, u, u + N, du, du + N, du + 2 * N);
     } else {

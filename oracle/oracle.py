@@ -37,8 +37,9 @@ class HexMesh(ctypes.Structure):
 
 class Model(ctypes.Structure):
     _fields_ = [("nx", I), ("nxi", I), ("ne", I), ("a", PD), ("b", PD), ("L", PD), ("sigma", PD),
-                ("eta", D), ("vpl", D), ("f0", D), ("v0", D), ("gamma", PD), ("n", PD),
-                ("deps0", D * 6), ("gf11_dft", PD), ("gf12", PD), ("gf21", PD), ("gf22", PD)]
+                ("eta", D), ("vpl", D), ("f0", D), ("v0", D), ("gamma", PD), ("n", PD), ("nlaws", I),
+                ("deps0", D * 6), ("tp", PD), ("deps", PD), ("beta", PD), ("p0", PD),
+                ("gf11_dft", PD), ("gf12", PD), ("gf21", PD), ("gf22", PD)]
 
 
 class SolverOpts(ctypes.Structure):
@@ -77,6 +78,7 @@ def lib():
             L.orc_gf_mm.argtypes = [ctypes.POINTER(HexMesh), D, D, PD, PD, I, PD]
             L.orc_ode_fault.argtypes = [ctypes.POINTER(Model)] + [PD] * 5
             L.orc_ode_visco.argtypes = [ctypes.POINTER(Model)] + [PD] * 8
+            L.orc_ode_dilatancy.argtypes = [ctypes.POINTER(Model)] + [PD] * 7
             L.orc_integrate.argtypes = [ctypes.POINTER(Model), PD, D, D, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)]
             L.orc_integrate.restype = I
             L.orc_gl_table.argtypes = [I, PD, PD]
@@ -178,7 +180,7 @@ def gf_mm(ma, lam, mu, quad=None):
 class OracleModel:
     """The reference's ODE parameter tuple (equation.jl:88,153) as an oracle model."""
 
-    def __init__(self, gf11, pf, gf12=None, gf21=None, gf22=None, pa=None):
+    def __init__(self, gf11, pf, gf12=None, gf21=None, gf22=None, pa=None, dila=None):
         self.keep = _Keep()
         nx, nxi, _ = gf11.shape
         ne = 0 if gf12 is None else gf12.shape[0] // 6
@@ -189,21 +191,36 @@ class OracleModel:
         flat = g.reshape(-1, order="F")
         gi[0::2], gi[1::2] = flat.real, flat.imag
         null = ctypes.cast(None, PD)
-        self.m = Model(nx, nxi, ne, self.keep(pf.a.reshape(-1, order="F")), self.keep(pf.b.reshape(-1, order="F")),
-                       self.keep(pf.L.reshape(-1, order="F")), self.keep(pf.σ.reshape(-1, order="F")),
+        F = lambda a: self.keep(np.asarray(a, dtype=np.float64).reshape(-1, order="F"))
+        if pa is not None and hasattr(pa, "piter"):  # CompositePowerLawViscosityProperty
+            gam = np.concatenate([np.asarray(q.γ, dtype=np.float64) for q in pa.piter])
+            nn = np.concatenate([np.asarray(q.n, dtype=np.float64) for q in pa.piter])
+            nlaws = len(pa.piter)
+        elif pa is not None:
+            gam, nn, nlaws = pa.γ, pa.n, 1
+        self.m = Model(nx, nxi, ne, F(pf.a), F(pf.b), F(pf.L), F(pf.σ),
                        pf.η, pf.vpl, pf.f0, pf.v0,
-                       self.keep(pa.γ) if pa is not None else null, self.keep(pa.n) if pa is not None else null,
-                       (D * 6)(*(pa.dϵ0 if pa is not None else np.zeros(6))), self.keep(gi),
+                       self.keep(gam) if pa is not None else null, self.keep(nn) if pa is not None else null,
+                       nlaws if pa is not None else 1,
+                       (D * 6)(*(pa.dϵ0 if pa is not None else np.zeros(6))),
+                       F(dila.tp) if dila is not None else null, F(dila.ϵ) if dila is not None else null,
+                       F(dila.β) if dila is not None else null, F(dila.p0) if dila is not None else null,
+                       self.keep(gi),
                        self.keep(gf12.reshape(-1, order="F")) if gf12 is not None else null,
                        self.keep(gf21.reshape(-1, order="F")) if gf21 is not None else null,
                        self.keep(gf22.reshape(-1, order="F")) if gf22 is not None else null)
         self.N, self.ne = nx * nxi, ne
+        self.dilatancy = dila is not None
 
     def ode(self, u):
-        """du for the flat state in ArrayPartition order (v, θ, [ϵ, σ,] δ)."""
+        """du for the flat state in ArrayPartition order (v, θ, [ϵ, σ,] δ) or (v, θ, δ, 𝓅)."""
         u = _c(u)
         du = np.zeros_like(u)
         N, E = self.N, 6 * self.ne
+        if self.dilatancy:
+            lib().orc_ode_dilatancy(ctypes.byref(self.m), _p(u[:N]), _p(u[N:2 * N]), _p(u[3 * N:]), _p(du[:N]),
+                                    _p(du[N:2 * N]), _p(du[2 * N:3 * N]), _p(du[3 * N:]))
+            return du
         if self.ne == 0:
             lib().orc_ode_fault(ctypes.byref(self.m), _p(u[:N]), _p(u[N:2 * N]), _p(du[:N]), _p(du[N:2 * N]), _p(du[2 * N:]))
         else:
@@ -222,7 +239,7 @@ class OracleModel:
 
     def integrate(self, u0, t0, t1, reltol=1e-6, abstol=1e-8, dt0=1e-8, dtmax=np.inf, dtmin=1e-14, maxiters=10**9):
         u = _c(u0).copy()
-        o = SolverOpts(reltol, abstol, dt0, dtmax, dtmin, maxiters, 1 if self.ne else 0)
+        o = SolverOpts(reltol, abstol, dt0, dtmax, dtmin, maxiters, 2 if self.dilatancy else (1 if self.ne else 0))
         s = SolverStats()
         lib().orc_integrate(ctypes.byref(self.m), _p(u), t0, t1, ctypes.byref(o), ctypes.byref(s))
         return u, s

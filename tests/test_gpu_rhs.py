@@ -173,3 +173,65 @@ def test_integrate_viscoelastic_matches_oracle(oracle):
     uc, sc = om.integrate(u, 0.0, T, reltol=1e-8, abstol=1e-10, dt0=1e-3)
     assert st.status == 0
     assert _rel(u1, uc) < 1e-6
+
+
+def test_rhs_dilatancy(oracle):
+    """assemble(gf, p, dila, u0, tspan) (equation.jl:108-117) and its ode (:168-183) vs the oracle."""
+    from oetqf_gb300 import ArrayPartition, DilatancyProperty, assemble
+    mf, gf, p = _fault(oracle, seed=8)
+    rng = np.random.default_rng(9)
+    sh = (mf.nx, mf.nξ)
+    dila = DilatancyProperty(*[rng.random(sh) for _ in range(4)])
+    u0 = ArrayPartition(*[rng.random(sh) for _ in range(4)])
+    prob = assemble(gf, p, dila, u0, (0.0, 1.0))
+    du = u0.similar()
+    prob.f(du, u0, prob.p, 1.0)
+    ref = oracle.OracleModel(gf, p, dila=dila).ode(u0.flat())
+    np.testing.assert_allclose(du.flat(), ref, rtol=RTOL, atol=1e-12 * np.abs(ref).max())
+
+
+def test_integrate_dilatancy_matches_oracle(oracle):
+    from oetqf_gb300 import DilatancyProperty
+    from oetqf_gb300.equation import GB300Model
+    mf = gen_mesh("RectOkada", 8e3, 4e3, 1e3, 1e3, 90.0)
+    mu = 3e10
+    N = mf.nx * mf.nξ
+    o = np.ones((mf.nx, mf.nξ))
+    pf = RateStateQuasiDynamicProperty(0.015 * o, 0.019 * o, 0.012 * o, 5e7 * o, mu / (2 * 3044.0), 1e-9, 0.6, 1e-6)
+    dila = DilatancyProperty(1e5 * o, 1e-4 * o, 1e-9 * o, 1e7 * o)
+    gf = oracle.gf_ff(mf, mu, mu, fourier=True)
+    m = GB300Model(mf.nx, mf.nξ, 0)
+    m.set_gf(1, gf)
+    m.set_fault_props(pf)
+    m.set_dilatancy(dila)
+    rng = np.random.default_rng(2)
+    u = np.concatenate([np.full(N, 1e-9), 0.012 / 1e-9 * (1 + 0.01 * rng.uniform(-1, 1, N)), np.zeros(N), np.full(N, 1e7)])
+    T = 0.1 * 3.15e7
+    u1, st = m.integrate(u, 0.0, T, reltol=1e-8, abstol=1e-10, dt=1e-3)
+    uc, sc = oracle.OracleModel(gf, pf, dila=dila).integrate(u, 0.0, T, reltol=1e-8, abstol=1e-10, dt0=1e-3)
+    assert st.status == 0 and sc.status == 0
+    assert _rel(u1, uc) < 1e-6
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_rhs_composite_viscosity(oracle, mode):
+    """CompositePowerLawViscosityProperty (property.jl:43-48, equation.jl:286-292) in FP64 and BF16."""
+    from oetqf_gb300 import CompositePowerLawViscosityProperty
+    from oetqf_gb300.equation import GB300Model
+    mf, ma, gfs, pf, pa = _visco(oracle, seed=12)
+    N, ne = mf.nx * mf.nξ, ma.ne
+    rng = np.random.default_rng(13)
+    laws = [PowerLawViscosityProperty(rng.random(ne), k * np.ones(ne), np.zeros(6)) for k in (0, 2)]
+    pc = CompositePowerLawViscosityProperty(laws, rng.random(6))
+    m = GB300Model(mf.nx, mf.nξ, ne)
+    for w, g in zip((1, 2, 3, 4), gfs):
+        m.set_gf(w, g)
+    m.set_fault_props(pf)
+    m.set_mantle_props(pc)
+    m.set_precision(mode)
+    u = rng.random(m.state_len)
+    du = m.rhs_flat(u)
+    ref = oracle.OracleModel(gfs[0], pf, *gfs[1:], pc).ode(u)
+    np.testing.assert_allclose(du[2 * N:2 * N + 6 * ne], ref[2 * N:2 * N + 6 * ne], rtol=1e-12)
+    if mode == 0:  # random friction inputs can overflow exp(); both sides must agree on those entries too
+        np.testing.assert_allclose(du, ref, rtol=RTOL, atol=1e-12 * np.nanmax(np.abs(ref)), equal_nan=True)

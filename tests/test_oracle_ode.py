@@ -117,3 +117,66 @@ def test_integrator_matches_scipy(oracle):
     assert st.status == 0 and st.t == T
     ref = scipy_integrate.solve_ivp(lambda t, y: m.ode(y), (0.0, T), u0, method="DOP853", rtol=1e-12, atol=1e-16)
     np.testing.assert_allclose(u1, ref.y[:, -1], rtol=1e-7)
+
+
+def test_composite_viscosity_law():
+    """test/BEM/tests.jl:150-153."""
+    from oetqf_gb300.property import CompositePowerLawViscosityProperty, dϵ_dt_composite
+    rng = np.random.default_rng(1)
+    A, n, σ, τ = rng.random(4)
+    p = PowerLawViscosityProperty([A], [n], rng.random(6))
+    A2, n2 = rng.random(2)
+    p2 = PowerLawViscosityProperty([A2], [n2], rng.random(6))
+    pc = CompositePowerLawViscosityProperty([p, p2], rng.random(6))
+    assert dϵ_dt_composite(pc, 0, σ, τ) == A * σ * τ ** n + A2 * σ * τ ** n2
+
+
+def test_okada_with_dilatancy_runs(oracle):
+    """test/BEM/tests.jl:73-82 with values: update_fault_with_dilatancy! (equation.jl:248-276) by hand."""
+    from oetqf_gb300.property import DilatancyProperty
+    mf, gf, p = _fault_model(oracle, seed=3)
+    rng = np.random.default_rng(4)
+    sh = (mf.nx, mf.nξ)
+    dila = DilatancyProperty(*[rng.random(sh) for _ in range(4)])
+    m = oracle.OracleModel(gf, p, dila=dila)
+    N = mf.nx * mf.nξ
+    u = rng.random(4 * N)
+    du = m.ode(u)
+    assert np.all(np.isfinite(du))
+    v, th, pp = u[:N], u[N:2 * N], u[3 * N:]
+    f = lambda a: a.reshape(-1, order="F")
+    a, b, L, s = f(p.a), f(p.b), f(p.L), f(p.σ)
+    tp, ep, be, p0 = f(dila.tp), f(dila.ϵ), f(dila.β), f(dila.p0)
+    dth = 1 - v * th / L
+    dp = -(pp - p0) / tp + ep / be / th * dth
+    af, bf = a / p.f0, b / p.f0
+    vf, thf = np.maximum(0, v / p.v0), np.maximum(0, th * p.v0 / L)
+    dtau = m.dtau_dt(v.reshape(sh, order="F"))
+    dv = (dtau + p.f0 * dp * vf**af * thf**bf - p.f0 * (s - pp) * vf**af * thf**(bf - 1) * bf * p.v0 / L * dth) / \
+         (p.f0 * (s - pp) * vf**(af - 1) * thf**bf * af / p.v0)
+    np.testing.assert_allclose(du[N:2 * N], dth, rtol=1e-14)
+    np.testing.assert_allclose(du[3 * N:], dp, rtol=1e-13)
+    np.testing.assert_allclose(du[:N], dv, rtol=1e-10)
+    np.testing.assert_array_equal(du[2 * N:3 * N], v)
+
+
+def test_composite_viscoelastic_rhs(oracle):
+    from oetqf_gb300.property import CompositePowerLawViscosityProperty
+    mf = gen_mesh("RectOkada", 100.0, 100.0, 10.0, 20.0, 90.0)
+    ma = gen_hex8_box(-100.0, -50.0, -20.0, 200.0, 100.0, -30.0, 2, 3, 4)
+    gfs = (oracle.gf_ff(mf, 1.0, 1.0, fourier=True), oracle.gf_fm(mf, ma, 1.0, 1.0), oracle.gf_mf(ma, mf, 1.0, 1.0),
+           oracle.gf_mm(ma, 1.0, 1.0))
+    rng = np.random.default_rng(6)
+    N, ne = mf.nx * mf.nξ, ma.ne
+    pf = RateStateQuasiDynamicProperty(*[rng.random((mf.nx, mf.nξ)) for _ in range(4)], *rng.random(4))
+    laws = [PowerLawViscosityProperty(rng.random(ne), k * np.ones(ne), np.zeros(6)) for k in (0, 2)]
+    pc = CompositePowerLawViscosityProperty(laws, rng.random(6))
+    u = rng.random(3 * N + 12 * ne)
+    du = oracle.OracleModel(gfs[0], pf, *gfs[1:], pc).ode(u)
+    sig = u[2 * N + 6 * ne:2 * N + 12 * ne].reshape((ne, 6), order="F")
+    skk = (sig[:, 0] + sig[:, 3] + sig[:, 5]) / 3
+    dev = sig.copy()
+    dev[:, [0, 3, 5]] -= skk[:, None]
+    tau = np.sqrt(dev[:, 0]**2 + dev[:, 3]**2 + dev[:, 5]**2 + 2 * (dev[:, 1]**2 + dev[:, 2]**2 + dev[:, 4]**2))
+    f = sum(q.γ * tau ** q.n for q in laws)
+    np.testing.assert_allclose(du[2 * N:2 * N + 6 * ne], (f[:, None] * dev).reshape(-1, order="F"), rtol=1e-13)
