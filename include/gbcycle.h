@@ -154,6 +154,13 @@ typedef struct gbc_solver_stats {
 /* Tsit5 with PI step control from t0 to t1; u (flat, host) is overwritten with u(t1). */
 int gbc_integrate(gbc_model* m, double* u, double t0, double t1, const gbc_solver_opts* opts,
                   gbc_solver_stats* stats);
+/* gbc_integrate that also records the state history like the reference's wsolve callback
+ * (src/io.jl:51-58, :118-133): record 0 is (t0, u0), then (t, u) after every stride-th accepted
+ * step, up to max_records (t_out: max_records, u_out: max_records x state_len, host). The device
+ * keeps a small ring of recent records that the host drains after each group of steps. */
+int gbc_integrate_record(gbc_model* m, double* u, double t0, double t1, const gbc_solver_opts* opts,
+                         int stride, long long max_records, double* t_out, double* u_out,
+                         long long* nrec, gbc_solver_stats* stats);
 /* Same with the state already on the device; does not synchronise the stats until it returns. */
 int gbc_integrate_dev(gbc_model* m, double* u_dev, double t0, double t1,
                       const gbc_solver_opts* opts, gbc_solver_stats* stats);

@@ -662,7 +662,7 @@ static int theta_transform(double* th, int n, int to_log, cudaStream_t s) {
 }
 
 static int integrate_common(gbc_model* m, double* u_dev, double t0, double t1, const gbc_solver_opts* o,
-                            gbc_solver_stats* st) {
+                            gbc_solver_stats* st, Recorder* rec = nullptr) {
     if (!o) return fail(GBC_EINVAL, "null solver options");
     if (!(o->reltol > 0) || !(o->abstol >= 0) || !(o->dt0 > 0) || !(o->dtmax > 0) || o->maxiters <= 0)
         return fail(GBC_EINVAL, "invalid solver options");
@@ -675,7 +675,7 @@ static int integrate_common(gbc_model* m, double* u_dev, double t0, double t1, c
         if (int rc = theta_transform(u_dev + m->N, m->N, 1, m->stream)) return rc;
     }
     int rc = integrator_run(m->integ, args, u_dev, t0, t1, o->reltol, o->abstol, o->dt0, o->dtmax,
-                            o->dtmin, o->maxiters, m->stream);
+                            o->dtmin, o->maxiters, m->stream, rec);
     if (args.log_theta) {
         if (int rc2 = theta_transform(u_dev + m->N, m->N, 0, m->stream)) return rc2;
     }
@@ -702,6 +702,28 @@ int gbc_integrate_dev(gbc_model* m, double* u_dev, double t0, double t1, const g
                       gbc_solver_stats* st) {
     if (!m || !u_dev) return fail(GBC_EINVAL, "null argument");
     return integrate_common(m, u_dev, t0, t1, o, st);
+}
+
+int gbc_integrate_record(gbc_model* m, double* u, double t0, double t1, const gbc_solver_opts* o, int stride,
+                         long long max_records, double* t_out, double* u_out, long long* nrec, gbc_solver_stats* st) {
+    if (!m || !u || !t_out || !u_out || !nrec) return fail(GBC_EINVAL, "null argument");
+    if (stride < 1 || max_records < 1) return fail(GBC_EINVAL, "stride and max_records must be positive");
+    const long long n = m->state_len();
+    // record 0: the initial state (the reference's callback also fires at t0)
+    t_out[0] = t0;
+    memcpy(u_out, u, sizeof(double) * n);
+    GBC_CUDA(cudaMemcpyAsync(m->u.p, u, sizeof(double) * n, cudaMemcpyHostToDevice, m->stream));
+    Recorder rec;
+    rec.stride = stride;
+    rec.max_records = max_records;
+    rec.t_out = t_out;
+    rec.u_out = u_out;
+    int rc = integrate_common(m, m->u.p, t0, t1, o, st, &rec);
+    *nrec = std::min(max_records, rec.drained + 1);
+    if (rc != 0 && rc != GBC_ESOLVER) return rc;
+    GBC_CUDA(cudaMemcpyAsync(u, m->u.p, sizeof(double) * n, cudaMemcpyDeviceToHost, m->stream));
+    GBC_CUDA(cudaStreamSynchronize(m->stream));
+    return rc;
 }
 
 int gbc_integrate(gbc_model* m, double* u, double t0, double t1, const gbc_solver_opts* o, gbc_solver_stats* st) {

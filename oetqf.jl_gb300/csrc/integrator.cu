@@ -99,6 +99,7 @@ __global__ void k_error_control(long long n, const double* __restrict__ u, const
         c->qold = fmax(EEst, 1e-4);
         c->naccept += 1;
         c->accept = 1;
+        c->record = (c->stride > 0 && c->naccept % c->stride == 0) ? 1 : 0;
         dtn = dt / q;
     } else {
         const double q = isfinite(q11) ? fmin(1.0 / qmin, q11 / gam) : 1.0 / qmin;
@@ -122,18 +123,29 @@ __global__ void k_error_control(long long n, const double* __restrict__ u, const
     c->dt = dtn;
 }
 
-// accept: u <- un and the FSAL derivative k0 <- k6
+// accept: u <- un and the FSAL derivative k0 <- k6; a recorded step also goes to the ring slot
+// nrec % ring_cap (θ restored from ψ when integrating ln θ)
 __global__ void k_commit(long long n, double* __restrict__ u, const double* __restrict__ un, double* __restrict__ k0,
                          const double* __restrict__ k6, const Ctrl* __restrict__ c) {
     if (!c->accept) return;
+    const bool rec = c->record && c->ring_cap > 0;
+    double* ur = rec ? c->u_ring + (c->nrec % c->ring_cap) * n : nullptr;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        u[i] = un[i];
+        const double v = un[i];
+        u[i] = v;
         k0[i] = k6[i];
+        if (rec) ur[i] = (c->log_theta && i >= c->th_lo && i < c->th_hi) ? exp(v) : v;
     }
+    if (rec && blockIdx.x == 0 && threadIdx.x == 0) c->t_ring[c->nrec % c->ring_cap] = c->t;
 }
 
 // the commit above must not run twice for one accepted step: clear the flag for the next step
-__global__ void k_clear_accept(Ctrl* c) { c->accept = 0; }
+// (and advance the ring after every block of k_commit has used the same slot)
+__global__ void k_clear_accept(Ctrl* c) {
+    if (c->accept && c->record && c->ring_cap > 0) c->nrec += 1;
+    c->accept = 0;
+    c->record = 0;
+}
 
 int integrator_alloc(Integrator& I, long long n) {
     if (I.n == n && I.y) return 0;
@@ -158,6 +170,8 @@ void integrator_free(Integrator& I) {
     if (I.ctrl) cudaFree(I.ctrl);
     if (I.ctrl_host) cudaFreeHost(I.ctrl_host);
     if (I.step_exec) cudaGraphExecDestroy(I.step_exec);
+    if (I.t_ring) cudaFree(I.t_ring);
+    if (I.u_ring) cudaFree(I.u_ring);
     I = Integrator();
 }
 
@@ -185,8 +199,23 @@ static int enqueue_step(Integrator& I, const RhsArgs& rhs0, double* u, cudaStrea
 
 int integrator_run(Integrator& I, const RhsArgs& rhs0, double* u, double t0, double t1, double reltol,
                    double abstol, double dt0, double dtmax, double dtmin, long long maxiters,
-                   cudaStream_t s) {
+                   cudaStream_t s, Recorder* rec) {
     Ctrl h{};
+    if (rec && rec->stride > 0) {
+        const long long cap = 32;  // >= the steps of one graph launch
+        if (I.ring_cap != cap) {
+            if (I.t_ring) cudaFree(I.t_ring);
+            if (I.u_ring) cudaFree(I.u_ring);
+            I.t_ring = I.u_ring = nullptr;
+            GBC_CUDA(cudaMalloc(&I.t_ring, sizeof(double) * cap));
+            GBC_CUDA(cudaMalloc(&I.u_ring, sizeof(double) * cap * I.n));
+            I.ring_cap = cap;
+        }
+        h.stride = rec->stride;
+        h.ring_cap = I.ring_cap;
+        h.t_ring = I.t_ring;
+        h.u_ring = I.u_ring;
+    }
     h.log_theta = rhs0.log_theta;
     h.th_lo = rhs0.N;
     h.th_hi = 2LL * rhs0.N;
@@ -228,6 +257,17 @@ int integrator_run(Integrator& I, const RhsArgs& rhs0, double* u, double t0, dou
         ++I.graph_launches;
         GBC_CUDA(cudaMemcpyAsync(I.ctrl_host, I.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s));
         GBC_CUDA(cudaStreamSynchronize(s));
+        if (rec && rec->stride > 0) {  // drain the ring into the caller's host arrays
+            const long long nrec = I.ctrl_host->nrec;
+            for (; rec->drained < nrec; ++rec->drained) {
+                const long long slot = rec->drained % I.ring_cap, dst = rec->drained + 1;  // slot 0 holds t0
+                if (dst >= rec->max_records) continue;
+                GBC_CUDA(cudaMemcpyAsync(rec->t_out + dst, I.t_ring + slot, sizeof(double), cudaMemcpyDeviceToHost, s));
+                GBC_CUDA(cudaMemcpyAsync(rec->u_out + dst * I.n, I.u_ring + slot * I.n, sizeof(double) * I.n,
+                                         cudaMemcpyDeviceToHost, s));
+            }
+            GBC_CUDA(cudaStreamSynchronize(s));
+        }
         if (I.ctrl_host->done) break;
     }
     return I.ctrl_host->status;

@@ -14,6 +14,19 @@ struct Ctrl {
     int done, status, accept, log_theta;
     unsigned int blocks_done;
     long long th_lo, th_hi;  // θ slot of the state; holds ψ = ln θ when log_theta
+    // recording (wsolve-style): every stride-th accepted step into a device ring of ring_cap slots
+    int stride, record;
+    long long nrec, ring_cap;
+    double* t_ring;
+    double* u_ring;
+};
+
+// host side of a recording: records are drained from the ring after each graph launch
+struct Recorder {
+    int stride = 0;
+    long long max_records = 0, drained = 0;
+    double* t_out = nullptr;   // host
+    double* u_out = nullptr;   // host, max_records x n
 };
 
 struct Integrator {
@@ -28,6 +41,9 @@ struct Integrator {
     cudaGraphExec_t step_exec = nullptr;  // captured group of steps
     int steps_per_launch = 0;
     long long graph_launches = 0;  // graph launches of the last run
+    double* t_ring = nullptr;      // device ring of the recorder (ring_cap slots)
+    double* u_ring = nullptr;
+    long long ring_cap = 0;
 };
 
 int integrator_alloc(Integrator& I, long long n);
@@ -35,6 +51,6 @@ void integrator_free(Integrator& I);
 // Integrates u (device) from t0 to t1. Fills the host mirror of Ctrl.
 int integrator_run(Integrator& I, const RhsArgs& rhs, double* u, double t0, double t1,
                    double reltol, double abstol, double dt0, double dtmax, double dtmin,
-                   long long maxiters, cudaStream_t s);
+                   long long maxiters, cudaStream_t s, Recorder* rec = nullptr);
 
 }  // namespace gbc

@@ -71,6 +71,8 @@ def lib():
             "gbc_rhs_dev": [P, D, P, P],
             "gbc_integrate": [P, PD, D, D, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
             "gbc_integrate_dev": [P, P, D, D, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
+            "gbc_integrate_record": [P, PD, D, D, ctypes.POINTER(SolverOpts), I, LL, PD, PD, ctypes.POINTER(LL),
+                                     ctypes.POINTER(SolverStats)],
             "gbc_last_error": [ctypes.c_char_p, ctypes.c_size_t],
             "gbc_model_set_log_theta": [P, I],
             "gbc_model_error_word": [P],

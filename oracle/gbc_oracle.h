@@ -111,6 +111,11 @@ typedef struct { long long naccept, nreject, nrhs; double t, dt; int status; } o
 int orc_integrate(const orc_model* m, double* u, double t0, double t1, const orc_solver_opts* o,
                   orc_solver_stats* st);
 long long orc_state_len(const orc_model* m, int mantle);
+/* orc_integrate that also records (t, u) at t0 and after every stride-th accepted step, as the
+ * reference's wsolve callback does (src/io.jl:51-58), up to max_records; *nrec gets the count. */
+int orc_integrate_record(const orc_model* m, double* u, double t0, double t1, const orc_solver_opts* o,
+                         orc_solver_stats* st, int stride, long long max_records, double* t_out,
+                         double* u_out, long long* nrec);
 int orc_num_threads(void);
 
 #ifdef __cplusplus

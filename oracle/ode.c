@@ -209,6 +209,12 @@ void orc_tsit5_tableau(double a[7][6], double e[7]) {
 
 int orc_integrate(const orc_model* m, double* u, double t0, double t1, const orc_solver_opts* o,
                   orc_solver_stats* stt) {
+    return orc_integrate_record(m, u, t0, t1, o, stt, 0, 0, NULL, NULL, NULL);
+}
+
+int orc_integrate_record(const orc_model* m, double* u, double t0, double t1, const orc_solver_opts* o,
+                         orc_solver_stats* stt, int stride, long long max_records, double* t_out,
+                         double* u_out, long long* nrec) {
     const long long n = orc_state_len(m, o->mantle);
     double* k[7];
     for (int s = 0; s < 7; ++s) k[s] = (double*)malloc(sizeof(double) * n);
@@ -223,6 +229,12 @@ int orc_integrate(const orc_model* m, double* u, double t0, double t1, const orc
     memset(stt, 0, sizeof(*stt));
     rhs_flat(m, o->mantle, u, k[0]);
     stt->nrhs = 1;
+    long long rec = 0;
+    if (stride > 0 && rec < max_records) {
+        t_out[rec] = t;
+        memcpy(u_out + rec * n, u, sizeof(double) * n);
+        ++rec;
+    }
     while (t < t1) {
         if (it++ >= o->maxiters) { status = -2; break; }
         if (dt > o->dtmax) dt = o->dtmax;
@@ -260,6 +272,11 @@ int orc_integrate(const orc_model* m, double* u, double t0, double t1, const orc
             qold = fmax(EEst, 1e-4);
             dt = dt / q;
             stt->naccept++;
+            if (stride > 0 && stt->naccept % stride == 0 && rec < max_records) {
+                t_out[rec] = t;
+                memcpy(u_out + rec * n, u, sizeof(double) * n);
+                ++rec;
+            }
         } else {
             double q = isfinite(q11) ? fmin(1.0 / qmin, q11 / gam) : 1.0 / qmin;
             dt = dt / q;
@@ -270,6 +287,7 @@ int orc_integrate(const orc_model* m, double* u, double t0, double t1, const orc
     stt->t = t;
     stt->dt = dt;
     stt->status = status;
+    if (nrec) *nrec = rec;
     for (int s = 0; s < 7; ++s) free(k[s]);
     free(y); free(un);
     return status;

@@ -81,6 +81,10 @@ def lib():
             L.orc_ode_dilatancy.argtypes = [ctypes.POINTER(Model)] + [PD] * 7
             L.orc_integrate.argtypes = [ctypes.POINTER(Model), PD, D, D, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)]
             L.orc_integrate.restype = I
+            L.orc_integrate_record.argtypes = [ctypes.POINTER(Model), PD, D, D, ctypes.POINTER(SolverOpts),
+                                               ctypes.POINTER(SolverStats), I, ctypes.c_longlong, PD, PD,
+                                               ctypes.POINTER(ctypes.c_longlong)]
+            L.orc_integrate_record.restype = I
             L.orc_gl_table.argtypes = [I, PD, PD]
             L.orc_num_threads.restype = I
             L.orc_dtau_dt.argtypes = [ctypes.POINTER(Model), PD, PD]
@@ -243,6 +247,21 @@ class OracleModel:
         s = SolverStats()
         lib().orc_integrate(ctypes.byref(self.m), _p(u), t0, t1, ctypes.byref(o), ctypes.byref(s))
         return u, s
+
+
+def integrate_record(om, u0, t0, t1, stride, max_records, reltol=1e-6, abstol=1e-8, dt0=1e-8, dtmax=np.inf,
+                     dtmin=1e-14, maxiters=10**9):
+    """orc_integrate_record: returns (u(t1), stats, t_records, u_records)."""
+    u = _c(u0).copy()
+    o = SolverOpts(reltol, abstol, dt0, dtmax, dtmin, maxiters, 2 if om.dilatancy else (1 if om.ne else 0))
+    s = SolverStats()
+    t_out = np.zeros(max_records)
+    u_out = np.zeros(max_records * u.size)
+    nrec = ctypes.c_longlong()
+    lib().orc_integrate_record(ctypes.byref(om.m), _p(u), t0, t1, ctypes.byref(o), ctypes.byref(s), stride,
+                               max_records, _p(t_out), _p(u_out), ctypes.byref(nrec))
+    k = nrec.value
+    return u, s, t_out[:k], u_out[:k * u.size].reshape(k, u.size)
 
 
 def tsit5_tableau():
