@@ -175,12 +175,14 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
         const double vi = v[i];
         const double ai = pa[i], bi = pb[i], Li = pL[i];
         if (m.log_theta) {
-            // ψ = ln θ: ψ1 = exp(c1 + (b/a) ψ), 1/θ = exp(-ψ); dψ = 1/θ - v/L; dμ/dθ dθ = b v ψ2 dψ
+            // ψ = ln θ: ψ1 = exp(c1 + (b/a) ψ), 1/θ = exp(-ψ); dψ = 1/θ - v/L; dμ/dθ dθ = b v ψ2 dψ;
+            // ψ2 = σ ψ1 / hypot(1, v ψ1) as one reciprocal square root
             const double psi = th[i];
-            const double psi1 = exp(pc[i] + (bi / ai) * psi);
-            const double psi2 = ps[i] * psi1 / sqrt(fma(vi * psi1, vi * psi1, 1.0));
-            const double dpsi = exp(-psi) - vi / Li;
-            k[i] = (dtau - bi * vi * psi2 * dpsi) / (ai * psi2 + m.eta);
+            const double psi1 = exp(fma(m.boa[i], psi, pc[i]));
+            const double vp = vi * psi1;
+            const double psi2 = ps[i] * psi1 * rsqrt(fma(vp, vp, 1.0));
+            const double dpsi = fma(-vi, m.iL[i], exp(-psi));
+            k[i] = fma(-bi * vi * psi2, dpsi, dtau) / fma(ai, psi2, m.eta);
             k[N + i] = dpsi;
         } else {
             const double tht = th[i];
@@ -498,8 +500,8 @@ struct gbc_ensemble {
     cudaStream_t stream = nullptr;
     EnsModel* d_models = nullptr;
     float* ghat = nullptr;
-    double *a = nullptr, *b = nullptr, *L = nullptr, *sig = nullptr, *c1 = nullptr, *u = nullptr, *y = nullptr,
-           *un = nullptr;
+    double *a = nullptr, *b = nullptr, *L = nullptr, *sig = nullptr, *c1 = nullptr, *boa = nullptr, *iL = nullptr,
+           *u = nullptr, *y = nullptr, *un = nullptr;
     double* k[7] = {};
     int block = 256;
     int max_cluster = 8;
@@ -517,7 +519,7 @@ int launch_gf_ff(const FaultDev& f, double lambda, double mu, int ftype, int nre
 static int ens_free(gbc_ensemble* e) {
     if (e->exec) cudaGraphExecDestroy(e->exec);
     ens_launch_destroy(e->lp);
-    void* ptrs[] = {e->d_models, e->ghat, e->a, e->b, e->L, e->sig, e->c1, e->u, e->y, e->un};
+    void* ptrs[] = {e->d_models, e->ghat, e->a, e->b, e->L, e->sig, e->c1, e->boa, e->iL, e->u, e->y, e->un};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int s = 0; s < 7; ++s)
@@ -594,7 +596,7 @@ int gbc_ensemble_create(int nmodels, const int* nx, const int* nxi, gbc_ensemble
     };
     A((void**)&e->d_models, sizeof(EnsModel) * nmodels);
     A((void**)&e->ghat, sizeof(float) * os);
-    for (double** p : {&e->a, &e->b, &e->L, &e->sig, &e->c1}) A((void**)p, sizeof(double) * on);
+    for (double** p : {&e->a, &e->b, &e->L, &e->sig, &e->c1, &e->boa, &e->iL}) A((void**)p, sizeof(double) * on);
     for (double** p : {&e->u, &e->y, &e->un}) A((void**)p, sizeof(double) * 3 * on);
     for (int s = 0; s < 7; ++s) A((void**)&e->k[s], sizeof(double) * 3 * on);
     if (!rc) rc = ens_launch_create(e->lp, nmodels);
@@ -602,6 +604,7 @@ int gbc_ensemble_create(int nmodels, const int* nx, const int* nxi, gbc_ensemble
     for (EnsModel& m : e->host) {
         m.ghat = e->ghat + m.off_st;
         m.a = e->a + m.off_n; m.b = e->b + m.off_n; m.L = e->L + m.off_n; m.sig = e->sig + m.off_n; m.c1 = e->c1 + m.off_n;
+        m.boa = e->boa + m.off_n; m.iL = e->iL + m.off_n;
         m.u = e->u + 3 * m.off_n; m.y = e->y + 3 * m.off_n; m.un = e->un + 3 * m.off_n;
         for (int s = 0; s < 7; ++s) m.k[s] = e->k[s] + 3 * m.off_n;
     }
@@ -707,9 +710,15 @@ int gbc_ensemble_set_fault_props(gbc_ensemble* e, int model, const double* a, co
     GBC_CUDA(cudaMemcpyAsync(e->b + m.off_n, b, sizeof(double) * N, cudaMemcpyHostToDevice, e->stream));
     GBC_CUDA(cudaMemcpyAsync(e->L + m.off_n, L, sizeof(double) * N, cudaMemcpyHostToDevice, e->stream));
     GBC_CUDA(cudaMemcpyAsync(e->sig + m.off_n, sigma, sizeof(double) * N, cudaMemcpyHostToDevice, e->stream));
-    std::vector<double> c1(N);
-    for (size_t i = 0; i < N; ++i) c1[i] = f0 / a[i] + (b[i] / a[i]) * std::log(v0 / L[i]) - std::log(2.0 * v0);
+    std::vector<double> c1(N), boa(N), iL(N);
+    for (size_t i = 0; i < N; ++i) {
+        c1[i] = f0 / a[i] + (b[i] / a[i]) * std::log(v0 / L[i]) - std::log(2.0 * v0);
+        boa[i] = b[i] / a[i];
+        iL[i] = 1.0 / L[i];
+    }
     GBC_CUDA(cudaMemcpyAsync(e->c1 + m.off_n, c1.data(), sizeof(double) * N, cudaMemcpyHostToDevice, e->stream));
+    GBC_CUDA(cudaMemcpyAsync(e->boa + m.off_n, boa.data(), sizeof(double) * N, cudaMemcpyHostToDevice, e->stream));
+    GBC_CUDA(cudaMemcpyAsync(e->iL + m.off_n, iL.data(), sizeof(double) * N, cudaMemcpyHostToDevice, e->stream));
     GBC_CUDA(cudaStreamSynchronize(e->stream));
     m.eta = eta; m.vpl = vpl; m.f0 = f0; m.v0 = v0;
     e->has_props[model] = 1;

@@ -15,6 +15,7 @@ struct EnsModel {
     // device buffers of this model
     const float* ghat;                       // real spectra of the circulant kernels (nxi, nxi, P/2+1)
     const double *a, *b, *L, *sig, *c1;      // friction (N each); c1 = f0/a + (b/a) ln(v0/L) - ln(2 v0)
+    const double *boa, *iL;                  // b/a and 1/L per patch (the ln θ friction path)
     double* u;                               // state (v, θ-or-ψ, δ), 3N
     double* k[7];                            // stage derivatives, 3N each
     double* y;                               // stage state

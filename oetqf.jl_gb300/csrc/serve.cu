@@ -91,7 +91,7 @@ struct gbc_server {
 
 static size_t fault_bytes(const Req& r, const EnsModel& m) {
     const size_t N = (size_t)m.N;
-    return sizeof(double) * ((size_t)m.nx * m.nxi * m.nxi + 5 * N + 30 * N) + sizeof(float) * ens_ghat_floats(m) + 4096;
+    return sizeof(double) * ((size_t)m.nx * m.nxi * m.nxi + 7 * N + 30 * N) + sizeof(float) * ens_ghat_floats(m) + 4096;
 }
 
 static size_t mantle_bytes(const Req& r) {
@@ -112,13 +112,13 @@ static int admit_fault(gbc_server* s, Req& r) {
     EnsModel& m = r.desc;
     if (int rc = ens_prepare_model(m, r.nx, r.nxi, &r.smem)) return rc;
     const size_t N = m.N, nst = (size_t)r.nx * r.nxi * r.nxi, ng = ens_ghat_floats(m);
-    const size_t nd = nst + 5 * N + 30 * N + 2 * (size_t)r.nx + 2 * (size_t)r.nxi + r.nx + 2 * (size_t)r.nxi;
+    const size_t nd = nst + 7 * N + 30 * N + 2 * (size_t)r.nx + 2 * (size_t)r.nxi + r.nx + 2 * (size_t)r.nxi;
     cudaStream_t st = s->admit;
     GBC_CUDA(cudaMallocAsync(&r.dmem, sizeof(double) * nd + sizeof(float) * ng + 256, st));
     double* d = static_cast<double*>(r.dmem);
     double* dst = d;
-    double *pa = dst + nst, *pb = pa + N, *pL = pb + N, *ps = pL + N, *pc = ps + N;
-    double* pu = pc + N;
+    double *pa = dst + nst, *pb = pa + N, *pL = pb + N, *ps = pL + N, *pc = ps + N, *pboa = pc + N, *piL = pboa + N;
+    double* pu = piL + N;
     double* pk = pu + 3 * N;          // 7 x 3N
     double* py = pk + 21 * N;
     double* pun = py + 3 * N;
@@ -128,8 +128,12 @@ static int admit_fault(gbc_server* s, Req& r) {
     auto up = [&](double* dd, const std::vector<double>& h) {
         return cudaMemcpyAsync(dd, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, st);
     };
-    std::vector<double> c1(N);
-    for (size_t i = 0; i < N; ++i) c1[i] = r.f0 / r.a[i] + (r.b[i] / r.a[i]) * std::log(r.v0 / r.L[i]) - std::log(2.0 * r.v0);
+    std::vector<double> c1(N), boa(N), iL(N);
+    for (size_t i = 0; i < N; ++i) {
+        c1[i] = r.f0 / r.a[i] + (r.b[i] / r.a[i]) * std::log(r.v0 / r.L[i]) - std::log(2.0 * r.v0);
+        boa[i] = r.b[i] / r.a[i];
+        iL[i] = 1.0 / r.L[i];
+    }
     cudaError_t e = cudaSuccess;
     for (auto pr : {std::make_pair(mx, &r.fx), std::make_pair(my, &r.fy), std::make_pair(mz, &r.fz),
                     std::make_pair(max_, &r.fax), std::make_pair(maxi, &r.faxi), std::make_pair(pa, &r.a),
@@ -137,6 +141,8 @@ static int admit_fault(gbc_server* s, Req& r) {
                     std::make_pair(pu, &r.u0)})
         if (e == cudaSuccess) e = up(pr.first, *pr.second);
     if (e == cudaSuccess) e = cudaMemcpyAsync(pc, c1.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(pboa, boa.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(piL, iL.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (admission)");
     FaultDev f{r.nx, r.nxi, mx, my, mz, max_, maxi, r.dx, r.dep, r.dip};
     if (int rc = launch_gf_ff(f, r.lambda, r.mu, r.ftype, r.nrept, r.buffer_ratio, dst, st)) return rc;
@@ -146,7 +152,7 @@ static int admit_fault(gbc_server* s, Req& r) {
     count_launches(3);
     GBC_CUDA(cudaStreamSynchronize(st));
     m.ghat = ghat;
-    m.a = pa; m.b = pb; m.L = pL; m.sig = ps; m.c1 = pc;
+    m.a = pa; m.b = pb; m.L = pL; m.sig = ps; m.c1 = pc; m.boa = pboa; m.iL = piL;
     m.u = pu; m.y = py; m.un = pun;
     for (int k = 0; k < 7; ++k) m.k[k] = pk + 3 * N * k;
     m.eta = r.eta; m.vpl = r.vpl; m.f0 = r.f0; m.v0 = r.v0;
