@@ -193,12 +193,14 @@ def run_gpu(args):
     m.set_fault_props(cm.pf)
     if cm.ne:
         m.set_mantle_props(cm.pa)
+    if args.storage == "df64":
+        m.set_precision(C.GBC_PREC_DF64)
     t_asm = time.perf_counter() - t_asm
     stream = torch.cuda.ExternalStream(m.stream)
     u = torch.tensor(cm.u0, device="cuda")
     if args.profile_rhs:
         if args.profile_precision != "f64":
-            m.set_precision(C.GBC_PREC_BF16 if args.profile_precision == "bf16" else C.GBC_PREC_F16)
+            m.set_precision({"bf16": C.GBC_PREC_BF16, "f16": C.GBC_PREC_F16, "df64": C.GBC_PREC_DF64}[args.profile_precision])
         du = torch.zeros_like(u)
         for _ in range(args.profile_rhs):
             m.rhs_dev(u.data_ptr(), du.data_ptr())
@@ -497,7 +499,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-rhs", type=int, default=0, help="run N right-hand sides only (for ncu captures)")
     ap.add_argument("--years", type=float, default=0.0, help="override the horizon (profiling runs only)")
-    ap.add_argument("--profile-precision", default="f64", choices=["f64", "bf16", "f16"])
+    ap.add_argument("--profile-precision", default="f64", choices=["f64", "bf16", "f16", "df64"])
+    ap.add_argument("--storage", default="f64", choices=["f64", "df64"],
+                    help="mantle Green's functions of the fault-mantle workloads: FP64, or FP32 pairs (FP64-accurate)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

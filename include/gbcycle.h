@@ -77,6 +77,8 @@ typedef struct gbc_model gbc_model;
 #define GBC_PREC_F64 0    /* Green's functions stored and applied in FP64 */
 #define GBC_PREC_BF16 1   /* block-scaled BF16 storage (128x128 FP32 scales), FP32 accumulate */
 #define GBC_PREC_F16 2    /* block-scaled FP16 storage (128x128 FP32 scales), FP32 accumulate */
+#define GBC_PREC_DF64 3   /* FP64-accurate double-float: each entry as an FP32 pair hi + lo, compensated
+                             FP32 products and sums (relative error ~1e-14), FP64 results */
 
 /* A model with nx*nxi fault patches and ne mantle cells (ne = 0: fault-only, equation.jl:156-166;
  * ne > 0: viscoelastic, equation.jl:185-205). Allocates device buffers; owns one CUDA stream. */
@@ -119,7 +121,11 @@ int gbc_model_export_gf(gbc_model* m, int which, double* host);
 /* Storage precision of the mantle Green's functions (GBC_PREC_*); FP64 by default. BF16/FP16
  * store [G12|G22] and G21 as one 16-bit matrix with an FP32 scale per 128x128 block and
  * accumulate in FP32; the fault-fault kernel runs in FP32 and friction stays FP64. The 16-bit
- * copy is rebuilt from the FP64 Green's functions whenever they change. */
+ * copy is rebuilt from the FP64 Green's functions whenever they change. DF64 stores the same
+ * rows as FP32 pairs (hi = fl32(g), lo = fl32(g - hi): the same 8 bytes per entry as FP64) and
+ * runs the dot products on the FP32 pipe with error-free transformations (TwoProduct by FMA,
+ * TwoSum), so the result keeps ~48 significant bits; the fault-fault sum and friction stay FP64.
+ * Entries and rates must lie inside FP32's normal range (1e-38 .. 3e38) for the full accuracy. */
 int gbc_model_set_precision(gbc_model* m, int mode);
 /* Integrate ψ = ln θ instead of θ inside gbc_integrate* (the caller's state keeps θ). */
 int gbc_model_set_log_theta(gbc_model* m, int on);

@@ -186,9 +186,11 @@ struct gbc_model {
         r.err = static_cast<int*>(err.p);
         return r;
     }
-    // builds the block-scaled 16-bit copies when the mixed mode is on and the GFs changed
+    // builds the block-scaled 16-bit (or double-float pair) copies when such a mode is on and the
+    // GFs changed
     int prepare() {
         if (precision == GBC_PREC_F64 || !mixed_dirty) return 0;
+        if (precision == GBC_PREC_DF64) return prepare_pairs();
         if (int rc = ready()) return rc;
         Mpad = (M + 127) / 128 * 128;
         rowsq = Mpad + (N + 127) / 128 * 128;
@@ -209,6 +211,26 @@ struct gbc_model {
                                          static_cast<float*>(qscale.p), s))
                 return rc;
             if (int rc = encode_qmap(precision, q.p, rowsq, ldq, tmap)) return rc;
+        }
+        GBC_CUDA(cudaStreamSynchronize(s));
+        mixed_dirty = false;
+        return 0;
+    }
+    int prepare_pairs() {
+        if (int rc = ready()) return rc;
+        cudaStream_t s = stream;
+        if (int rc = err.alloc(sizeof(int))) return rc;
+        GBC_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+        if (ne > 0) {
+            Mpad = (M + 127) / 128 * 128;
+            rowsq = Mpad + (N + 127) / 128 * 128;
+            ldq = (npad + M + 255) / 256 * 256;
+            if (int rc = q.alloc(8 * (size_t)rowsq * ldq)) return rc;
+            if (int rc = x32.alloc(8 * (size_t)ldq)) return rc;
+            GBC_CUDA(cudaMemsetAsync(x32.p, 0, 8 * (size_t)ldq, s));
+            if (int rc = split_mantle(nx, nxi, npad, M, Mpad, rowsq, ldq, st.p, gm.p, ldm, g21.p, ld21, q.p, s))
+                return rc;
+            if (int rc = encode_pairmap(q.p, rowsq, ldq, tmap)) return rc;
         }
         GBC_CUDA(cudaStreamSynchronize(s));
         mixed_dirty = false;
@@ -592,7 +614,7 @@ int gbc_model_assemble(gbc_model* m, const gbc_fault_mesh* mf, const gbc_hex_mes
 
 int gbc_model_set_precision(gbc_model* m, int mode) {
     if (!m) return fail(GBC_EINVAL, "null model");
-    if (mode != GBC_PREC_F64 && mode != GBC_PREC_BF16 && mode != GBC_PREC_F16)
+    if (mode != GBC_PREC_F64 && mode != GBC_PREC_BF16 && mode != GBC_PREC_F16 && mode != GBC_PREC_DF64)
         return fail(GBC_EINVAL, "unknown precision mode");
     if (mode != m->precision) m->mixed_dirty = true;
     m->precision = mode;

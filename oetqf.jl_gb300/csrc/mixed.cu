@@ -19,6 +19,7 @@
 
 #include "gbc_internal.cuh"
 #include "rhs.cuh"
+#include "tma.cuh"
 
 namespace gbc {
 
@@ -28,7 +29,6 @@ constexpr int TC = 256;        // columns per TMA tile (512 B of 16-bit)
 constexpr int STAGES = 4;
 constexpr unsigned kTileBytes = TR * TC * 2;
 constexpr unsigned kXBytes = TC * 4;
-constexpr long long kWaitLimit = 1LL << 24;
 
 // ---- quantisation --------------------------------------------------------------------------
 struct QSrc {
@@ -127,47 +127,6 @@ int encode_qmap(int mode, void* q, long long rowsq, long long ldq, void* tmap_ou
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(GBC_ECUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
     return 0;
-}
-
-// ---- mbarrier / TMA helpers ----------------------------------------------------------------
-__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// bounded wait: false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
-    for (long long i = 0; i < kWaitLimit; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-__device__ __forceinline__ void tma_tile(void* dst, const CUtensorMap* tm, int c0, int c1, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
-        : "memory");
-}
-__device__ __forceinline__ void bulk_copy(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
 }
 
 template <int MODE>
@@ -277,13 +236,25 @@ __global__ void __launch_bounds__(256) k_gemv_tma(const __grid_constant__ CUtens
     }
 }
 
-// FP32 x = [v - vpl; 0; dϵ - dϵ₀] and dϵ (FP64) -- the viscoelastic prologue of the mixed path
+// x = [v - vpl; 0; dϵ - dϵ₀] in FP32 (PAIR: as FP32 pairs hi + lo) and dϵ (FP64) -- the
+// viscoelastic prologue of the 16-bit and double-float paths
+template <bool PAIR>
+__device__ __forceinline__ void put_x(float* x, long long i, double v) {
+    if (PAIR) {
+        const float hi = __double2float_rn(v);
+        reinterpret_cast<float2*>(x)[i] = make_float2(hi, __double2float_rn(v - (double)hi));
+    } else {
+        x[i] = (float)v;
+    }
+}
+
+template <bool PAIR>
 __global__ void k_prologue_mixed(RhsArgs a, const double* __restrict__ u, double* __restrict__ du, StateLayout L) {
     if (a.skip && *a.skip) return;
     const int ne = a.ne, N = a.N;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N + ne; t += gridDim.x * blockDim.x) {
         if (t < N) {
-            a.x32[t] = (float)(u[L.v + t] - a.vpl);
+            put_x<PAIR>(a.x32, t, u[L.v + t] - a.vpl);
             continue;
         }
         const int i = t - N;
@@ -292,14 +263,13 @@ __global__ void k_prologue_mixed(RhsArgs a, const double* __restrict__ u, double
         const double sxx = s[i] - skk, syy = s[i + 3 * ne] - skk, szz = s[i + 5 * ne] - skk;
         const double sxy = s[i + ne], sxz = s[i + 2 * ne], syz = s[i + 4 * ne];
         const double tau = sqrt(sxx * sxx + syy * syy + szz * szz + 2.0 * (sxy * sxy + sxz * sxz + syz * syz));
-        double f = 0.0;
-        for (int q = 0; q < a.nlaws; ++q) f += a.gamma[i + (size_t)q * ne] * pow(tau, a.nexp[i + (size_t)q * ne]);
+        const double f = viscous_factor(a, i, tau);
         const double d[6] = {f * sxx, f * sxy, f * sxz, f * syy, f * syz, f * szz};
         double* deps = du + L.eps;
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
             deps[i + k * ne] = d[k];
-            a.x32[a.npad + i + k * ne] = (float)(d[k] - a.deps0[k]);
+            put_x<PAIR>(a.x32, a.npad + i + (long long)k * ne, d[k] - a.deps0[k]);
         }
     }
 }
@@ -312,7 +282,6 @@ __global__ void __launch_bounds__(256) k_fault_rows_mixed(RhsArgs a, const doubl
     const int warps = gridDim.x * (blockDim.x >> 5);
     const int nx = a.nx, nxi = a.nxi, N = a.N;
     const double* v = u + L.v;
-    const float vpl = (float)a.vpl;
     for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < N; i += warps) {
         const int ii = i % nx, j = i / nx;
         float acc = 0.f;
@@ -325,32 +294,24 @@ __global__ void __launch_bounds__(256) k_fault_rows_mixed(RhsArgs a, const doubl
             }
         }
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        (void)vpl;
-        if (lane == 0) {
-            const double dtau = (double)acc + (a.ne > 0 ? (double)a.y32[i] : 0.0);
-            const double vi = v[i], th = a.log_theta ? exp(u[L.th + i]) : u[L.th + i];
-            const double ai = a.a[i], bi = a.b[i], Li = a.L[i];
-            const double psi1 = exp((a.f0 + bi * log(a.v0 * fmax(0.0, th) / Li)) / ai) / (2.0 * a.v0);
-            const double psi2 = a.sig[i] * psi1 / hypot(1.0, vi * psi1);
-            const double dmu_dv = ai * psi2;
-            const double dmu_dth = bi / th * vi * psi2;
-            const double dth = 1.0 - vi * th / Li;
-            du[L.th + i] = a.log_theta ? dth / th : dth;
-            du[L.v + i] = (dtau - dmu_dth * dth) / (dmu_dv + a.eta);
-            du[L.delta + i] = vi;
-        }
+        if (lane == 0) fault_friction(a, u, du, L, i, (double)acc + (a.ne > 0 ? (double)a.y32[i] : 0.0));
     }
 }
 
 int launch_rhs_mixed(const RhsArgs& a, const double* u, double* du, cudaStream_t s) {
     const StateLayout L = layout_of(a.N, a.ne);
     const int sms = sm_count();
+    const bool pair = (a.mode == GBC_PREC_DF64);
     if (a.ne > 0) {
         const int n = a.N + a.ne;
         int g = (n + 255) / 256;
         if (g > sms * 8) g = sms * 8;
-        k_prologue_mixed<<<g, 256, 0, s>>>(a, u, du, L);
+        if (pair) k_prologue_mixed<true><<<g, 256, 0, s>>>(a, u, du, L);
+        else k_prologue_mixed<false><<<g, 256, 0, s>>>(a, u, du, L);
         GBC_CUDA(cudaGetLastError());
+    }
+    if (pair) return launch_gemv_df64(a, u, du, s);  // fault rows and friction included
+    if (a.ne > 0) {
         const size_t smem = STAGES * (kTileBytes + kXBytes) + 2 * STAGES * sizeof(uint64_t);
         const unsigned grid = (unsigned)(a.rowsq / TR);
         CUtensorMap tm;

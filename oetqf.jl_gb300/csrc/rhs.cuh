@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <cstddef>
 
+#include "gbcycle.h"
+
 namespace gbc {
 
 struct RhsArgs {
@@ -33,13 +35,13 @@ struct RhsArgs {
     // integrate ln θ instead of θ (the state's θ slot holds ψ = ln θ; dψ/dt = (1 - vθ/L)/θ)
     int log_theta;
     // ---- block-scaled 16-bit storage (GBC_PREC_BF16 / GBC_PREC_F16) --------------------------
-    int mode;                    // 0: FP64 path above; 1: BF16; 2: FP16
+    int mode;                    // GBC_PREC_*: 0 FP64 path above; 1 BF16; 2 FP16; 3 double-float pairs
     const void* q;               // (rowsq x ldq) 16-bit: rows [0,M) = [G12|0|G22], [Mpad,Mpad+N) = [0|G21]
     const float* qscale;         // FP32 scale per 128x128 block, (rowsq/128) x (ldq/128)
     long long rowsq, ldq, Mpad;
     const void* tmap;            // host pointer to the CUtensorMap of q (box 256 x 32)
     const float* st32;           // fault-fault Toeplitz kernel in FP32
-    float* x32;                  // [v - vpl; 0; dϵ - dϵ₀; 0] in FP32, length ldq
+    float* x32;                  // [v - vpl; 0; dϵ - dϵ₀; 0] in FP32, length ldq (DF64: FP32 pairs, 2 ldq)
     float* y32;                  // G21 part of the fault rows, length N
     int* err;                    // device error word (bounded-wait timeouts)
 };
@@ -74,6 +76,34 @@ inline StateLayout layout_of(int N, int ne, int dila = 0) {
     return s;
 }
 
+#ifdef __CUDACC__
+// update_fault! (equation.jl:233-246) with the ageing law (:279) for patch i, given its traction
+// rate dτ: writes dθ (or dψ = dθ/θ when the state holds ψ = ln θ), dv and dδ = v.
+__device__ __forceinline__ void fault_friction(const RhsArgs& a, const double* __restrict__ u, double* __restrict__ du,
+                                               const StateLayout& L, int i, double dtau) {
+    const double vi = u[L.v + i], th = a.log_theta ? exp(u[L.th + i]) : u[L.th + i];
+    const double ai = a.a[i], bi = a.b[i], Li = a.L[i];
+    const double psi1 = exp((a.f0 + bi * log(a.v0 * fmax(0.0, th) / Li)) / ai) / (2.0 * a.v0);
+    const double psi2 = a.sig[i] * psi1 / hypot(1.0, vi * psi1);
+    const double dmu_dv = ai * psi2;
+    const double dmu_dth = bi / th * vi * psi2;
+    const double dth = 1.0 - vi * th / Li;
+    du[L.th + i] = a.log_theta ? dth / th : dth;
+    du[L.v + i] = (dtau - dmu_dth * dth) / (dmu_dv + a.eta);
+    du[L.delta + i] = vi;
+}
+
+// Σ_q γ_q τ^{n_q} of cell i (equation.jl:285-292); τ^0 = 1 exactly, as pow returns
+__device__ __forceinline__ double viscous_factor(const RhsArgs& a, int i, double tau) {
+    double f = 0.0;
+    for (int q = 0; q < a.nlaws; ++q) {
+        const double n = a.nexp[i + (size_t)q * a.ne];
+        f += a.gamma[i + (size_t)q * a.ne] * (n == 0.0 ? 1.0 : pow(tau, n));
+    }
+    return f;
+}
+#endif
+
 // Launches the RHS for the flat state u -> du on stream s (1 kernel fault-only, 2 viscoelastic).
 int launch_rhs(const RhsArgs& a, const double* u, double* du, cudaStream_t s);
 // Number of kernels one launch_rhs enqueues for these arguments.
@@ -88,5 +118,16 @@ int quantize_mantle(int mode, int N, int npad, long long M, long long Mpad, long
 // Encodes the TMA descriptor for q (rowsq x ldq 16-bit, box 256 columns x 32 rows).
 int encode_qmap(int mode, void* q, long long rowsq, long long ldq, void* tmap_out /* 128 B */);
 int fault_f32(const double* st, float* st32, long long n, cudaStream_t s);
+
+// Double-float path (df64.cu): q holds (rowsq x ldq) FP32 pairs of the unified rows, whose fault
+// rows carry the dense fault-fault block expanded from the Toeplitz kernel st in columns [0, N).
+int split_mantle(int nx, int nxi, int npad, long long M, long long Mpad, long long rowsq, long long ldq,
+                 const double* st, const double* gm, size_t ldm, const double* g21, size_t ld21, void* q,
+                 cudaStream_t s);
+int encode_pairmap(void* q, long long rowsq, long long ldq, void* tmap_out /* 128 B */);
+// The double-float GEMV over all unified rows; fault rows finish with the friction update.
+int launch_gemv_df64(const RhsArgs& a, const double* u, double* du, cudaStream_t s);
+// the path launch_rhs takes: FP64 rows, or the 16-bit / double-float mantle GEMV
+inline bool uses_mixed(const RhsArgs& a) { return a.mode != 0 && !a.dila && !(a.mode == GBC_PREC_DF64 && a.ne == 0); }
 
 }  // namespace gbc

@@ -65,8 +65,7 @@ __global__ void k_prologue(RhsArgs a, const double* __restrict__ u, double* __re
         const double sxx = s[i] - skk, syy = s[i + 3 * ne] - skk, szz = s[i + 5 * ne] - skk;
         const double sxy = s[i + ne], sxz = s[i + 2 * ne], syz = s[i + 4 * ne];
         const double tau = sqrt(sxx * sxx + syy * syy + szz * szz + 2.0 * (sxy * sxy + sxz * sxz + syz * syz));
-        double f = 0.0;  // equation.jl:285 (one law) or :286-292 (composite: sum of laws)
-        for (int q = 0; q < a.nlaws; ++q) f += a.gamma[i + (size_t)q * ne] * pow(tau, a.nexp[i + (size_t)q * ne]);
+        const double f = viscous_factor(a, i, tau);  // equation.jl:285 (one law) or :286-292 (composite)
         const double d[6] = {f * sxx, f * sxy, f * sxz, f * syy, f * syz, f * szz};
         double* deps = du + L.eps;
 #pragma unroll
@@ -120,27 +119,19 @@ __global__ void __launch_bounds__(256) k_rows(RhsArgs a, const double* __restric
                           (a.f0 * (a.sig[i] - pi) * vfa1 * thfb * af / a.v0);
             du[L.delta + i] = vi;
         } else if (lane == 0) {
-            const double vi = v[i], th = a.log_theta ? exp(u[L.th + i]) : u[L.th + i];
-            const double ai = a.a[i], bi = a.b[i], Li = a.L[i];
-            const double psi1 = exp((a.f0 + bi * log(a.v0 * fmax(0.0, th) / Li)) / ai) / (2.0 * a.v0);
-            const double psi2 = a.sig[i] * psi1 / hypot(1.0, vi * psi1);
-            const double dmu_dv = ai * psi2;
-            const double dmu_dth = bi / th * vi * psi2;
-            const double dth = 1.0 - vi * th / Li;
-            du[L.th + i] = a.log_theta ? dth / th : dth;
-            du[L.v + i] = (dtau - dmu_dth * dth) / (dmu_dv + a.eta);
-            du[L.delta + i] = vi;
+            fault_friction(a, u, du, L, i, dtau);
         }
     }
 }
 
 int rhs_kernel_count(const RhsArgs& a) {
-    if (a.mode != 0 && !a.dila) return a.ne > 0 ? 3 : 1;
+    if (uses_mixed(a) && a.mode == GBC_PREC_DF64) return 2;
+    if (uses_mixed(a)) return a.ne > 0 ? 3 : 1;
     return a.ne > 0 ? 2 : 1;
 }
 
 int launch_rhs(const RhsArgs& a, const double* u, double* du, cudaStream_t s) {
-    if (a.mode != 0 && !a.dila) return launch_rhs_mixed(a, u, du, s);
+    if (uses_mixed(a)) return launch_rhs_mixed(a, u, du, s);
     const StateLayout L = layout_of(a.N, a.ne, a.dila);
     const int sms = sm_count();
     if (a.ne > 0) {

@@ -15,7 +15,7 @@ I = ctypes.c_int
 LL = ctypes.c_longlong
 
 GBC_STRIKE_SLIP, GBC_DIP_SLIP = 0, 1
-GBC_PREC_F64, GBC_PREC_BF16, GBC_PREC_F16 = 0, 1, 2
+GBC_PREC_F64, GBC_PREC_BF16, GBC_PREC_F16, GBC_PREC_DF64 = 0, 1, 2, 3
 GBC_GF11_REAL, GBC_GF11_DFT, GBC_GF12, GBC_GF21, GBC_GF22 = 0, 1, 2, 3, 4
 ERRORS = {-1: "EINVAL", -2: "ENODEV", -3: "ECUDA", -4: "ENOMEM", -5: "ESOLVER", -6: "ESTATE"}
 
