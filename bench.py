@@ -41,7 +41,8 @@ SOLVER = dict(reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=0.2 * YEAR)
 STEPS_FOR_HORIZON = {"fault-mantle-1000x2500-f64": 42388, "fault-800-f64": 4757}
 # DRAM bytes (read + write) of one k_rows launch from ncu, per workload
 # (profiles/k_rows_fault-mantle-1000x2500-f64.md)
-NCU_TRAFFIC = {"fault-mantle-1000x2500-f64": 2044237000 + 2987264}
+NCU_TRAFFIC = {"fault-mantle-1000x2500-f64": 2044237000 + 2987264,
+               "fault-mantle-1000x2500-f64-df64": 2081574000 + 3372032}
 
 
 def workload(name):
@@ -264,7 +265,38 @@ def run_gpu(args):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = rhs_bytes(cm) / (rhs_ms / 1e3) / 1e9
-    traffic = NCU_TRAFFIC.get(args.workload)
+    traffic = NCU_TRAFFIC.get(args.workload + ("-df64" if args.storage == "df64" else ""))
+    df64_line = None
+    if cm.ne and args.storage == "f64":
+        # the FP64-accurate double-float storage, one RHS timed the same way (the FP64 pipe bounds
+        # the FP64 GEMV; the FP32-pair GEMV is bound by HBM)
+        m.set_precision(C.GBC_PREC_DF64)
+        for _ in range(3):
+            m.rhs_dev(u.data_ptr(), du.data_ptr())
+        d0, d1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        d0.record(stream)
+        for _ in range(R):
+            m.rhs_dev(u.data_ptr(), du.data_ptr())
+        d1.record(stream)
+        d1.synchronize()
+        dms = d0.elapsed_time(d1) / R
+        m.set_precision(C.GBC_PREC_F64)
+        da = rhs_bytes(cm) / (dms / 1e3) / 1e9
+        df64_line = {"kernel": "k_prologue_mixed + k_gemv_df64 (one RHS)", "rhs_ms": dms, "achieved": da, "peak": peak,
+                     "unit": "GB/s", "frac": da / peak, "speedup_vs_f64_rhs": rhs_ms / dms,
+                     "run": "python bench.py --storage df64"}
+    err_vs_f64 = None
+    if args.storage == "df64":
+        # slip-rate agreement with the plain FP64 path over one year from the initial state
+        from oetqf_gb300.equation import GB300Model as _M
+        ref = _M(cm.mf.nx, cm.mf.nξ, cm.ne)
+        ref.assemble_gf(cm.mf, cm.ma, cm.lam, cm.mu)
+        ref.set_fault_props(cm.pf)
+        ref.set_mantle_props(cm.pa)
+        ua, _ = ref.integrate(cm.u0, 0.0, YEAR, **SOLVER)
+        ub, _ = m.integrate(cm.u0, 0.0, YEAR, **SOLVER)
+        err_vs_f64 = float(np.abs(ub[:cm.N] - ua[:cm.N]).max() / np.abs(ua[:cm.N]).max())
+        del ref
     # e2e: the same horizon through the host-buffer C-ABI call (pinned host state, H2D + D2H per window)
     uh = torch.tensor(cm.u0).pin_memory()
     un = uh.numpy()
@@ -280,18 +312,27 @@ def run_gpu(args):
     if rank != 0:
         return
     line = {"metric": "sim-yr/s", "value": value, "unit": "sim-yr/s", "n_gpus": ws, "steps": K, "warmup": args.warmup,
-            "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.storage == "f64" else "f32x2 (double-float pairs, FP64-accurate)",
             "data": "synthetic (seeded splitmix64)",
             "config": {"workload": args.workload, "fault_patches": cm.N, "mantle_cells": cm.ne, "horizon_yr": sim_yr,
-                       "precision": "f64", "solver": "Tsit5 reltol 1e-6 abstol 1e-8 dt0 1e-8 s dtmax 0.2 yr",
+                       "precision": "f64" if args.storage == "f64" else
+                       "mantle + fault rows as FP32 pairs (hi + lo), compensated FP32 dot products, FP64 results and friction",
+                       "solver": "Tsit5 reltol 1e-6 abstol 1e-8 dt0 1e-8 s dtmax 0.2 yr",
                        "l2": "inputs larger than L2 (Green's functions read every RHS)", "parallelism": "replicas",
                        "rk_steps": naccept + nreject, "rk_rejected": nreject, "assembly_s": round(t_asm, 3)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "kernel": "k_prologue + k_rows (one RHS)", "rhs_ms": rhs_ms,
+                         "traffic": traffic, "rhs_ms": rhs_ms,
+                         "kernel": "k_prologue + k_rows (one RHS)" if args.storage == "f64" else
+                         "k_prologue_mixed + k_gemv_df64 (one RHS)",
                          "bytes_per_launch": rhs_bytes(cm), "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"},
             "e2e": {"value": sim_yr / (e2e_ms / 1e3), "unit": "sim-yr/s", "h2d_bytes_per_step": int(cm.u0.nbytes),
                     "d2h_bytes_per_step": int(cm.u0.nbytes)},
             "clocks": clk, "gpu_launches": launches}
+    if df64_line:
+        line["roofline_df64"] = df64_line
+    if err_vs_f64 is not None:
+        line["max_slip_rate_rel_err_vs_f64_1yr"] = err_vs_f64
     if not args.no_cpu:
         gfs = tuple(m.export_gf(w) for w in (C.GBC_GF12, C.GBC_GF21, C.GBC_GF22)) if cm.ne else None
         line["cpu_baseline"] = cpu_oracle_sample(cm, args.workload, gfs=gfs, budget_s=args.cpu_budget)
