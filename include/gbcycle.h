@@ -270,8 +270,11 @@ typedef struct gbc_request_result {
 
 typedef struct gbc_server_info {
     int queued, batched, mantle;
-    double bytes_in_use, peak_bytes;
+    double bytes_in_use, peak_bytes;   /* bytes_in_use includes cached Green's functions */
     long long iterations;
+    int cache_entries;                 /* assembled geometries resident on the device */
+    double cache_bytes;
+    long long cache_hits, cache_misses;
 } gbc_server_info;
 
 /* A server admitting requests while their estimated device footprint fits hbm_budget_bytes
@@ -281,6 +284,12 @@ int gbc_server_submit(gbc_server* s, const gbc_request* req, long long* id);
 /* Blocks until request id finishes; writes its final state into u_out (host, may be NULL). */
 int gbc_server_wait(gbc_server* s, long long id, double* u_out, gbc_request_result* res);
 int gbc_server_query(gbc_server* s, gbc_server_info* out);
+/* Green's-function cache across requests (on by default; the serving counterpart of saving and
+ * reloading assembled Green's functions, examples/otf-with-mantle.jl:44-56): requests whose mesh,
+ * elastic constants, fault type, images, buffer ratio, quadrature and precision equal a cached
+ * geometry skip assembly. Idle entries count against the budget and are evicted least recently
+ * used first. Turning it off frees the idle entries. */
+int gbc_server_set_gf_cache(gbc_server* s, int enabled);
 /* Finishes every admitted and queued request, then stops the scheduler. */
 void gbc_server_destroy(gbc_server* s);
 

@@ -8,6 +8,12 @@
 //    its descriptor), so results are bitwise the same alone and in the mix.
 //  * Requests with a mantle run on their own model stream in a worker thread (block-scaled BF16
 //    Green's functions, ln θ state); their kernels overlap with the batch on the device.
+//  * Assembled Green's functions are cached on the device, keyed by the exact bytes of everything
+//    they depend on (mesh, elastic constants, fault type, images, buffer ratio, quadrature and
+//    storage precision): fault-only requests share one read-only spectrum buffer per geometry,
+//    mantle requests take an idle assembled model of their geometry (its FP64 and 16-bit copies)
+//    and skip assembly. Idle entries stay resident and count against the HBM budget; admission
+//    evicts them least recently used first when the next request would not fit otherwise.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -42,8 +48,11 @@ struct Req {
     std::vector<double> u0, u1;
     double t0 = 0, t1 = 0;
     gbc_solver_opts opts{};
-    // bookkeeping
-    size_t footprint = 0;
+    // bookkeeping: own bytes (state, properties) plus the Green's-function part, charged only when
+    // the geometry is not cached
+    size_t own = 0, gf = 0;
+    std::string key;
+    struct GfEntry* entry = nullptr;
     double t_submit = 0, t_admit = 0, t_done = 0;
     int status = 0;
     bool done = false;
@@ -57,9 +66,45 @@ struct Req {
     bool worker_done = false;
 };
 
+// A cached geometry: the spectra of a fault-only geometry, or an assembled model with a mantle.
+struct GfEntry {
+    std::string key;
+    bool mantle = false;
+    bool valid = false;        // assembly finished successfully
+    float* ghat = nullptr;     // fault-only
+    gbc_model* model = nullptr;  // mantle: FP64 + storage-precision Green's functions, state buffers
+    size_t bytes = 0;
+    int refs = 0;
+    double last = 0;
+};
+
+static void key_put(std::string& k, const void* p, size_t n) { k.append(static_cast<const char*>(p), n); }
+static void key_vec(std::string& k, const std::vector<double>& v) {
+    const size_t n = v.size();
+    key_put(k, &n, sizeof(n));
+    if (n) key_put(k, v.data(), sizeof(double) * n);
+}
+static std::string gf_key(const Req& r) {
+    std::string k(1, r.ne > 0 ? 'M' : 'F');
+    const int ints[5] = {r.nx, r.nxi, r.ne, r.ftype, r.nrept};
+    const double d[7] = {r.dx, r.dxi, r.dep, r.dip, r.lambda, r.mu, r.buffer_ratio};
+    key_put(k, ints, sizeof(ints));
+    key_put(k, d, sizeof(d));
+    for (const auto* v : {&r.fx, &r.fxi, &r.fy, &r.fz, &r.fax, &r.faxi}) key_vec(k, *v);
+    if (r.ne > 0) {
+        for (int j = 0; j < 9; ++j) key_vec(k, r.hex[j]);
+        key_vec(k, r.qc);
+        key_vec(k, r.qw);
+        key_put(k, &r.precision, sizeof(r.precision));
+    }
+    return k;
+}
+
 }  // namespace gbc
 
 using namespace gbc;
+
+extern "C" void gbc_model_destroy(gbc_model*);
 
 struct gbc_server {
     double budget = 0;
@@ -83,15 +128,21 @@ struct gbc_server {
     std::chrono::steady_clock::time_point t_start;
     long long iterations = 0;
     std::string fatal;
+    std::vector<std::unique_ptr<GfEntry>> cache;
+    bool cache_on = true;
+    long long hits = 0, misses = 0;
 
     double now() const {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
     }
 };
 
-static size_t fault_bytes(const Req& r, const EnsModel& m) {
-    const size_t N = (size_t)m.N;
-    return sizeof(double) * ((size_t)m.nx * m.nxi * m.nxi + 7 * N + 30 * N) + sizeof(float) * ens_ghat_floats(m) + 4096;
+// own: properties, c1, b/a, 1/L (7N) and state, stages, candidate (30N); gf: the spectra plus the
+// transient FP64 Toeplitz kernel and mesh they are computed from
+static size_t fault_own_bytes(const EnsModel& m) { return sizeof(double) * 37 * (size_t)m.N + 4096; }
+static size_t fault_gf_bytes(const Req& r, const EnsModel& m) {
+    return sizeof(double) * ((size_t)m.nx * m.nxi * m.nxi + 3 * (size_t)r.nx + 4 * (size_t)r.nxi) +
+           sizeof(float) * ens_ghat_floats(m) + 512;
 }
 
 static size_t mantle_bytes(const Req& r) {
@@ -110,24 +161,37 @@ __global__ void k_theta_one(double* th, int n, int to_log) {
 
 static int admit_fault(gbc_server* s, Req& r) {
     EnsModel& m = r.desc;
+    GfEntry* ge = r.entry;
     if (int rc = ens_prepare_model(m, r.nx, r.nxi, &r.smem)) return rc;
     const size_t N = m.N, nst = (size_t)r.nx * r.nxi * r.nxi, ng = ens_ghat_floats(m);
-    const size_t nd = nst + 7 * N + 30 * N + 2 * (size_t)r.nx + 2 * (size_t)r.nxi + r.nx + 2 * (size_t)r.nxi;
     cudaStream_t st = s->admit;
-    GBC_CUDA(cudaMallocAsync(&r.dmem, sizeof(double) * nd + sizeof(float) * ng + 256, st));
-    double* d = static_cast<double*>(r.dmem);
-    double* dst = d;
-    double *pa = dst + nst, *pb = pa + N, *pL = pb + N, *ps = pL + N, *pc = ps + N, *pboa = pc + N, *piL = pboa + N;
+    auto up = [&](double* dd, const std::vector<double>& h) {
+        return cudaMemcpyAsync(dd, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, st);
+    };
+    if (!ge->valid) {  // first request of this geometry: its spectra, from a transient FP64 kernel
+        double* tmp = nullptr;
+        GBC_CUDA(cudaMallocAsync(&tmp, sizeof(double) * (nst + 3 * (size_t)r.nx + 4 * (size_t)r.nxi), st));
+        GBC_CUDA(cudaMallocAsync(&ge->ghat, sizeof(float) * ng, st));
+        double* mx = tmp + nst;  // mesh: x (nx), y, z (nxi), ax (2nx), axi (2nxi)
+        double *my = mx + r.nx, *mz = my + r.nxi, *max_ = mz + r.nxi, *maxi = max_ + 2 * r.nx;
+        cudaError_t e = cudaSuccess;
+        for (auto pr : {std::make_pair(mx, &r.fx), std::make_pair(my, &r.fy), std::make_pair(mz, &r.fz),
+                        std::make_pair(max_, &r.fax), std::make_pair(maxi, &r.faxi)})
+            if (e == cudaSuccess) e = up(pr.first, *pr.second);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (mesh)");
+        FaultDev f{r.nx, r.nxi, mx, my, mz, max_, maxi, r.dx, r.dep, r.dip};
+        if (int rc = launch_gf_ff(f, r.lambda, r.mu, r.ftype, r.nrept, r.buffer_ratio, tmp, st)) return rc;
+        if (int rc = ens_ghat(tmp, m, ge->ghat, st)) return rc;
+        count_launches(2);
+        GBC_CUDA(cudaFreeAsync(tmp, st));
+    }
+    GBC_CUDA(cudaMallocAsync(&r.dmem, sizeof(double) * 37 * N + 256, st));
+    double* pa = static_cast<double*>(r.dmem);
+    double *pb = pa + N, *pL = pb + N, *ps = pL + N, *pc = ps + N, *pboa = pc + N, *piL = pboa + N;
     double* pu = piL + N;
     double* pk = pu + 3 * N;          // 7 x 3N
     double* py = pk + 21 * N;
     double* pun = py + 3 * N;
-    double* mx = pun + 3 * N;         // mesh: x (nx), y, z (nxi), ax (2nx), axi (2nxi)
-    double *my = mx + r.nx, *mz = my + r.nxi, *max_ = mz + r.nxi, *maxi = max_ + 2 * r.nx;
-    float* ghat = reinterpret_cast<float*>(maxi + 2 * r.nxi);
-    auto up = [&](double* dd, const std::vector<double>& h) {
-        return cudaMemcpyAsync(dd, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, st);
-    };
     std::vector<double> c1(N), boa(N), iL(N);
     for (size_t i = 0; i < N; ++i) {
         c1[i] = r.f0 / r.a[i] + (r.b[i] / r.a[i]) * std::log(r.v0 / r.L[i]) - std::log(2.0 * r.v0);
@@ -135,23 +199,17 @@ static int admit_fault(gbc_server* s, Req& r) {
         iL[i] = 1.0 / r.L[i];
     }
     cudaError_t e = cudaSuccess;
-    for (auto pr : {std::make_pair(mx, &r.fx), std::make_pair(my, &r.fy), std::make_pair(mz, &r.fz),
-                    std::make_pair(max_, &r.fax), std::make_pair(maxi, &r.faxi), std::make_pair(pa, &r.a),
-                    std::make_pair(pb, &r.b), std::make_pair(pL, &r.L), std::make_pair(ps, &r.sig),
-                    std::make_pair(pu, &r.u0)})
+    for (auto pr : {std::make_pair(pa, &r.a), std::make_pair(pb, &r.b), std::make_pair(pL, &r.L),
+                    std::make_pair(ps, &r.sig), std::make_pair(pu, &r.u0), std::make_pair(pc, &c1),
+                    std::make_pair(pboa, &boa), std::make_pair(piL, &iL)})
         if (e == cudaSuccess) e = up(pr.first, *pr.second);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(pc, c1.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(pboa, boa.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(piL, iL.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (admission)");
-    FaultDev f{r.nx, r.nxi, mx, my, mz, max_, maxi, r.dx, r.dep, r.dip};
-    if (int rc = launch_gf_ff(f, r.lambda, r.mu, r.ftype, r.nrept, r.buffer_ratio, dst, st)) return rc;
-    if (int rc = ens_ghat(dst, m, ghat, st)) return rc;
     k_theta_one<<<(int)((N + 255) / 256), 256, 0, st>>>(pu + N, (int)N, 1);
     GBC_CUDA(cudaGetLastError());
-    count_launches(3);
+    count_launches(1);
     GBC_CUDA(cudaStreamSynchronize(st));
-    m.ghat = ghat;
+    ge->valid = true;
+    m.ghat = ge->ghat;
     m.a = pa; m.b = pb; m.L = pL; m.sig = ps; m.c1 = pc; m.boa = pboa; m.iL = piL;
     m.u = pu; m.y = py; m.un = pun;
     for (int k = 0; k < 7; ++k) m.k[k] = pk + 3 * N * k;
@@ -188,7 +246,6 @@ static void finish_fault(gbc_server* s, Req& r) {
 
 // ---- mantle requests --------------------------------------------------------------------------
 extern "C" int gbc_model_create(int, int, int, gbc_model**);
-extern "C" void gbc_model_destroy(gbc_model*);
 extern "C" int gbc_model_assemble(gbc_model*, const gbc_fault_mesh*, const gbc_hex_mesh*, double, double, int, int,
                                   double, const double*, const double*, int);
 extern "C" int gbc_model_set_fault_props(gbc_model*, const double*, const double*, const double*, const double*, double,
@@ -200,33 +257,97 @@ extern "C" int gbc_integrate(gbc_model*, double*, double, double, const gbc_solv
 
 static void run_mantle(gbc_server* s, std::shared_ptr<Req> rp) {
     Req& r = *rp;
-    gbc_model* m = nullptr;
-    int rc = gbc_model_create(r.nx, r.nxi, r.ne, &m);
-    gbc_fault_mesh mf{r.nx, r.nxi, r.fx.data(), r.fxi.data(), r.fy.data(), r.fz.data(), r.fax.data(), r.faxi.data(),
-                      r.dx, r.dxi, r.dep, r.dip};
-    gbc_hex_mesh ma{r.ne, r.hex[0].data(), r.hex[1].data(), r.hex[2].data(), r.hex[3].data(), r.hex[4].data(),
-                    r.hex[5].data(), r.hex[6].data(), r.hex[7].data(), r.hex[8].data()};
-    if (!rc) rc = gbc_model_assemble(m, &mf, &ma, r.lambda, r.mu, r.ftype, r.nrept, r.buffer_ratio,
-                                     r.qc.empty() ? nullptr : r.qc.data(), r.qw.empty() ? nullptr : r.qw.data(),
-                                     (int)r.qw.size());
+    GfEntry* ge = r.entry;  // exclusively this request's while it runs (refs == 1)
+    gbc_model* m = ge->model;
+    int rc = 0;
+    bool assembled = ge->valid;
+    if (!assembled) {
+        rc = gbc_model_create(r.nx, r.nxi, r.ne, &m);
+        gbc_fault_mesh mf{r.nx, r.nxi, r.fx.data(), r.fxi.data(), r.fy.data(), r.fz.data(), r.fax.data(),
+                          r.faxi.data(), r.dx, r.dxi, r.dep, r.dip};
+        gbc_hex_mesh ma{r.ne, r.hex[0].data(), r.hex[1].data(), r.hex[2].data(), r.hex[3].data(), r.hex[4].data(),
+                        r.hex[5].data(), r.hex[6].data(), r.hex[7].data(), r.hex[8].data()};
+        if (!rc) rc = gbc_model_assemble(m, &mf, &ma, r.lambda, r.mu, r.ftype, r.nrept, r.buffer_ratio,
+                                         r.qc.empty() ? nullptr : r.qc.data(), r.qw.empty() ? nullptr : r.qw.data(),
+                                         (int)r.qw.size());
+        if (!rc) rc = gbc_model_set_precision(m, r.precision);
+        assembled = (rc == 0);
+    }
     if (!rc) rc = gbc_model_set_fault_props(m, r.a.data(), r.b.data(), r.L.data(), r.sig.data(), r.eta, r.vpl, r.f0, r.v0);
     if (!rc) rc = gbc_model_set_mantle_props(m, r.gamma.data(), r.nexp.data(), r.deps0);
-    if (!rc) rc = gbc_model_set_precision(m, r.precision);
     if (!rc) rc = gbc_model_set_log_theta(m, r.precision != GBC_PREC_F64);
     r.u1 = r.u0;
     if (!rc) rc = gbc_integrate(m, r.u1.data(), r.t0, r.t1, &r.opts, &r.stats);
-    if (m) gbc_model_destroy(m);
     std::lock_guard<std::mutex> lk(s->mu);
+    ge->model = m;
+    ge->valid = assembled;
     r.status = rc;
     r.worker_done = true;
     s->cv.notify_all();
 }
 
 // ---- scheduler ----------------------------------------------------------------------------------
-static void complete(gbc_server* s, Req& r) {  // holds s->mu
+// the following hold s->mu
+static void drop_entry(gbc_server* s, GfEntry* e) {
+    if (e->ghat) cudaFreeAsync(e->ghat, s->admit);
+    if (e->model) gbc_model_destroy(e->model);
+    s->in_use -= e->bytes;
+    for (size_t i = 0; i < s->cache.size(); ++i)
+        if (s->cache[i].get() == e) { s->cache.erase(s->cache.begin() + i); break; }
+}
+
+// evicts idle entries, least recently used first, until `need` more bytes fit; false if they cannot
+static bool make_room(gbc_server* s, size_t need) {
+    while (s->in_use + need > s->budget) {
+        GfEntry* victim = nullptr;
+        for (auto& e : s->cache)
+            if (e->refs == 0 && (!victim || e->last < victim->last)) victim = e.get();
+        if (!victim) return false;
+        drop_entry(s, victim);
+    }
+    return true;
+}
+
+// takes a cached entry for request r (or makes a new one) and charges the budget; false: no room yet
+static bool acquire(gbc_server* s, Req& r) {
+    GfEntry* hit = nullptr;
+    if (s->cache_on)
+        for (auto& e : s->cache)
+            if (e->valid && e->key == r.key && (!e->mantle || e->refs == 0)) { hit = e.get(); break; }
+    const size_t need = r.own + (hit ? 0 : r.gf);
+    if (hit) ++hit->refs;  // pinned: make_room never evicts it
+    if (!make_room(s, need)) {
+        if (hit) --hit->refs;
+        return false;
+    }
+    s->in_use += need;
+    if (hit) {
+        ++s->hits;
+        r.entry = hit;
+    } else {
+        ++s->misses;
+        auto e = std::make_unique<GfEntry>();
+        e->key = r.key;
+        e->mantle = r.ne > 0;
+        e->bytes = r.gf;
+        e->refs = 1;
+        r.entry = e.get();
+        s->cache.push_back(std::move(e));
+    }
+    r.entry->last = s->now();
+    return true;
+}
+
+static void complete(gbc_server* s, Req& r) {
     r.t_done = s->now();
     r.done = true;
-    s->in_use -= r.footprint;
+    s->in_use -= r.own;
+    if (GfEntry* e = r.entry) {
+        --e->refs;
+        e->last = r.t_done;
+        if (e->refs == 0 && (!e->valid || !s->cache_on)) drop_entry(s, e);
+        r.entry = nullptr;
+    }
     s->done_cv.notify_all();
 }
 
@@ -234,11 +355,11 @@ static void scheduler(gbc_server* s) {
     cudaSetDevice(0);
     std::unique_lock<std::mutex> lk(s->mu);
     while (true) {
-        // admit from the head of the queue while the HBM budget allows (arrival order)
-        while (!s->queue.empty() && s->in_use + s->queue.front()->footprint <= s->budget) {
+        // admit from the head of the queue while the HBM budget allows (arrival order); cached
+        // Green's functions are reused, idle ones evicted when the head would not fit otherwise
+        while (!s->queue.empty() && acquire(s, *s->queue.front())) {
             std::shared_ptr<Req> r = s->queue.front();
             s->queue.pop_front();
-            s->in_use += r->footprint;
             s->peak = std::max(s->peak, s->in_use);
             r->t_admit = s->now();
             if (r->ne > 0) {
@@ -251,6 +372,7 @@ static void scheduler(gbc_server* s) {
                 if (rc) {
                     r->status = rc;
                     if (r->dmem) { cudaFreeAsync(r->dmem, s->admit); r->dmem = nullptr; }
+                    cudaStreamSynchronize(s->admit);
                     complete(s, *r);
                 } else {
                     s->batch_active.push_back(r);
@@ -364,15 +486,18 @@ int gbc_server_submit(gbc_server* s, const gbc_request* q, long long* id) {
         for (int k = 0; k < 6; ++k) r->deps0[k] = q->deps0[k];
         if (q->nq > 0) { r->qc.assign(q->qcoords, q->qcoords + 3 * q->nq); r->qw.assign(q->qweights, q->qweights + q->nq); }
         r->u0.assign(q->u0, q->u0 + 3 * N + 12 * (size_t)r->ne);
-        r->footprint = mantle_bytes(*r);
+        r->own = 0;  // the assembled model holds the state too
+        r->gf = mantle_bytes(*r);
     } else {
         EnsModel m;
         size_t smem;
         if (int rc = ens_prepare_model(m, r->nx, r->nxi, &smem)) return rc;
         r->u0.assign(q->u0, q->u0 + 3 * N);
-        r->footprint = fault_bytes(*r, m);
+        r->own = fault_own_bytes(m);
+        r->gf = fault_gf_bytes(*r, m);
     }
-    if ((double)r->footprint > s->budget) return fail(GBC_ENOMEM, "request larger than the server's HBM budget");
+    r->key = gf_key(*r);
+    if ((double)(r->own + r->gf) > s->budget) return fail(GBC_ENOMEM, "request larger than the server's HBM budget");
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stop) return fail(GBC_ESTATE, "server is shutting down");
     r->id = s->next_id++;
@@ -413,6 +538,22 @@ int gbc_server_query(gbc_server* s, gbc_server_info* out) {
     out->bytes_in_use = (double)s->in_use;
     out->peak_bytes = (double)s->peak;
     out->iterations = s->iterations;
+    out->cache_entries = (int)s->cache.size();
+    double cb = 0;
+    for (auto& e : s->cache) cb += (double)e->bytes;
+    out->cache_bytes = cb;
+    out->cache_hits = s->hits;
+    out->cache_misses = s->misses;
+    return 0;
+}
+
+int gbc_server_set_gf_cache(gbc_server* s, int enabled) {
+    if (!s) return fail(GBC_EINVAL, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->cache_on = enabled != 0;
+    if (!s->cache_on)
+        for (size_t i = s->cache.size(); i-- > 0;)
+            if (s->cache[i]->refs == 0) drop_entry(s, s->cache[i].get());
     return 0;
 }
 
@@ -424,6 +565,10 @@ void gbc_server_destroy(gbc_server* s) {
         s->cv.notify_all();
     }
     if (s->sched.joinable()) s->sched.join();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        while (!s->cache.empty()) drop_entry(s, s->cache.back().get());
+    }
     if (s->d_desc) cudaFree(s->d_desc);
     ens_launch_destroy(s->lp);
     cudaStreamSynchronize(s->batch);

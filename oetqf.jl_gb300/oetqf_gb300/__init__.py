@@ -6,15 +6,17 @@ side (src/BEM/equation.jl), and an on-device adaptive integrator. Compute runs i
 """
 from .mesh import (BEMHex8Mesh, RectOkadaMesh, gauss1_quadrature, gauss_product_quadrature, gen_hex8_box,
                    gen_mesh, sincosd)
+from .persist import load_greens_functions, save_greens_functions
 from .property import (CompositePowerLawViscosityProperty, DilatancyProperty, PowerLawViscosityProperty,
-                       RateStateQuasiDynamicProperty, dϵ_dt, dϵ_dt_composite)
+                       RateStateQuasiDynamicProperty, dϵ_dt, dϵ_dt_composite, load_property, save_property)
 
 import unicodedata as _ud
 
 __all__ = ["BEMHex8Mesh", "RectOkadaMesh", "gen_mesh", "gen_hex8_box", "gauss1_quadrature", "gauss_product_quadrature",
            "sincosd", "RateStateQuasiDynamicProperty", "PowerLawViscosityProperty", "CompositePowerLawViscosityProperty",
            "DilatancyProperty", "dϵ_dt", "dϵ_dt_composite", "stress_greens_function",
-           "StrikeSlip", "DipSlip", "assemble", "solve", "ArrayPartition", "GB300Model", "ODEProblem"]
+           "StrikeSlip", "DipSlip", "assemble", "solve", "ArrayPartition", "GB300Model", "ODEProblem",
+           "save_property", "load_property", "save_greens_functions", "load_greens_functions"]
 # identifiers are NFKC-normalised (ϵ -> ε); keep the exported names in that form
 __all__ = [_ud.normalize("NFKC", n) for n in __all__]
 

@@ -114,6 +114,22 @@ class GB300Model:
         C.check(C.lib().gbc_model_assemble(self.h, ctypes.byref(fs), ctypes.byref(hs) if hs is not None else None,
                                            lam, mu, _ftype(ftype), nrept, buffer_ratio, k(qc), k(qw), len(qw)))
 
+    def save_gf(self, file: str) -> None:
+        """Write this model's Green's functions (gf₁₁ as the complex rFFT form) to a file."""
+        from .persist import save_greens_functions
+        g = {"gf11": self.export_gf(C.GBC_GF11_DFT)}
+        if self.ne:
+            g.update(gf12=self.export_gf(C.GBC_GF12), gf21=self.export_gf(C.GBC_GF21), gf22=self.export_gf(C.GBC_GF22))
+        save_greens_functions(file, **g)
+
+    def load_gf(self, file: str) -> None:
+        """Set this model's Green's functions from a file written by save_gf (no assembly)."""
+        from .persist import load_greens_functions
+        g = load_greens_functions(file)
+        which = {"gf11": C.GBC_GF11_DFT, "gf12": C.GBC_GF12, "gf21": C.GBC_GF21, "gf22": C.GBC_GF22}
+        for k, v in g.items():
+            self.set_gf(which[k], v)
+
     def export_gf(self, which: int) -> np.ndarray:
         N, M = self.N, 6 * self.ne
         shape = {C.GBC_GF11_REAL: (self.nx, self.nξ, self.nξ), C.GBC_GF12: (M, N), C.GBC_GF21: (N, M),

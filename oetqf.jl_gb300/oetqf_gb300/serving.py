@@ -34,7 +34,8 @@ class RequestResult(ctypes.Structure):
 
 class ServerInfo(ctypes.Structure):
     _fields_ = [("queued", C.I), ("batched", C.I), ("mantle", C.I), ("bytes_in_use", C.D), ("peak_bytes", C.D),
-                ("iterations", ctypes.c_longlong)]
+                ("iterations", ctypes.c_longlong), ("cache_entries", C.I), ("cache_bytes", C.D),
+                ("cache_hits", ctypes.c_longlong), ("cache_misses", ctypes.c_longlong)]
 
 
 def _sigs():
@@ -48,6 +49,8 @@ def _sigs():
     L.gbc_server_wait.restype = C.I
     L.gbc_server_query.argtypes = [P, ctypes.POINTER(ServerInfo)]
     L.gbc_server_query.restype = C.I
+    L.gbc_server_set_gf_cache.argtypes = [P, C.I]
+    L.gbc_server_set_gf_cache.restype = C.I
     L.gbc_server_destroy.argtypes = [P]
     L.gbc_server_destroy.restype = None
     return L
@@ -102,6 +105,10 @@ class Server:
         if rc < 0 and rc != -5:
             C.check(rc)
         return u, res
+
+    def set_gf_cache(self, enabled: bool):
+        """Keep assembled Green's functions on the device across requests (default on)."""
+        C.check(C.lib().gbc_server_set_gf_cache(self.h, int(bool(enabled))))
 
     def info(self) -> ServerInfo:
         i = ServerInfo()

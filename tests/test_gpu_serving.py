@@ -66,3 +66,56 @@ def test_server_matches_standalone_ensemble():
     u, st = e.integrate(u0, 0.0, [r.horizon for r in reqs])
     for i, r in enumerate(reqs):
         np.testing.assert_array_equal(got[i], u[e.offsets[i]:e.offsets[i] + r.u0.size])
+
+
+def _same_geometry(cm, scale):
+    """The request cm with the same mesh and elastic constants, other friction and initial state."""
+    import copy
+    r = copy.deepcopy(cm)
+    r.pf.a = r.pf.a * scale
+    r.u0 = r.u0.copy()
+    r.u0[:r.N] *= scale
+    return r
+
+
+def test_gf_cache_reuses_geometry_and_keeps_results():
+    """Fault-only and mantle requests on one geometry: later requests hit the cache and give the
+    bitwise result of a server that assembles every request itself."""
+    from oetqf_gb300.serving import Server
+    base = fault_ensemble(n_models=1, years=0.5, n_range=(200, 300), seed=19)[0]
+    mant = serving_requests(n_requests=8, seed=23, mantle_fraction=1.0, patch_range=(100, 200), cell_range=(8, 27),
+                            year_range=(0.2, 0.4))[0]
+    assert mant.ma is not None
+    reqs = [base, _same_geometry(base, 1.01), _same_geometry(base, 0.99), mant, _same_geometry(mant, 1.02)]
+    out = {}
+    for cache in (True, False):
+        s = Server(hbm_budget_gb=8.0)
+        s.set_gf_cache(cache)
+        got = []
+        for r in reqs:  # one at a time: a mantle model is reused only when idle
+            got.append(s.wait(s.submit(r))[0])
+        info = s.info()
+        s.close()
+        out[cache] = (got, info)
+    got_c, info_c = out[True]
+    got_n, info_n = out[False]
+    for a, b in zip(got_c, got_n):
+        np.testing.assert_array_equal(a, b)
+    assert (info_c.cache_hits, info_c.cache_misses) == (3, 2)
+    assert info_c.cache_entries == 2 and info_c.cache_bytes > 0
+    assert info_n.cache_hits == 0 and info_n.cache_entries == 0
+
+
+def test_gf_cache_evicts_idle_geometries_under_budget():
+    from oetqf_gb300.serving import Server
+    reqs = fault_ensemble(n_models=4, years=0.2, n_range=(300, 400), seed=29)
+    budget = 0.00025  # 268 KB: a request (156-171 KB) and one or two idle geometries (54-57 KB each)
+    s = Server(hbm_budget_gb=budget)
+    for r in reqs:
+        u, res = s.wait(s.submit(r))
+        assert res.status == 0
+    info = s.info()
+    s.close()
+    assert info.peak_bytes <= budget * 2**30
+    assert info.cache_hits + info.cache_misses == 4
+    assert info.cache_entries < info.cache_misses  # an idle geometry was evicted to admit a later one
