@@ -46,6 +46,7 @@ struct EnsSmem {
     float2* Z;
     float2* X;
     float2* tw;
+    double* part;  // error-norm sums of this rank's 32-patch chunks
 };
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
@@ -111,8 +112,11 @@ template <int BS>
 __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, const EnsSmem& S,
                                         const double* __restrict__ y, double* __restrict__ k, int lo, int hi,
                                         cooperative_groups::cluster_group& cl) {
-    // every rank's slice of y (the stage state) must be visible before the full slip-rate vector is read
-    cl.sync();
+    // every rank's slice of y (the stage state) must be visible before the full slip-rate vector is
+    // read; a one-CTA model only needs its own writes, which a CTA barrier orders without the
+    // cluster barrier's release/acquire fence
+    if (cl.num_blocks() > 1) cl.sync();
+    else __syncthreads();
     const int N = m.N, nx = m.nx, nxi = m.nxi, P = m.P, logP = m.logP, H = P / 2 + 1;
     const int nq = (nxi + 1) / 2;
     const double* v = y;
@@ -222,12 +226,17 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
     const EnsModel m = M;  // sizes, constants and the step control state at launch
     if (m.done) return;    // the same descriptor for every rank: cluster-uniform
     const int N = m.N;
-    const int lo = (int)((long long)N * rank / csize), hi = (int)((long long)N * (rank + 1) / csize);
+    // each rank owns whole 32-patch chunks, so the error norm below sums the same chunks in the
+    // same order whatever the cluster and block sizes: a model's trajectory does not depend on them
+    const int nch = (N + 31) / 32;
+    const int lo = 32 * (int)((long long)nch * rank / csize);
+    const int hi = min(N, 32 * (int)((long long)nch * (rank + 1) / csize));
     const int nq = (m.nxi + 1) / 2, H = m.P / 2 + 1;
     EnsSmem S;
     S.Z = reinterpret_cast<float2*>(sm);
     S.X = S.Z + (size_t)nq * m.P;
     S.tw = S.X + (size_t)m.nxi * H;
+    S.part = reinterpret_cast<double*>(S.tw + m.P / 2);
     for (int t = threadIdx.x; t < m.P / 2; t += BS) {
         double sn, cs;
         sincospi(2.0 * t / m.P, &sn, &cs);
@@ -251,64 +260,103 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
     }
     for (int step = 0; step < A.budget; ++step) {
         // stop decision of rank 0 (completion or the launch's wall-clock budget), shared through L2
-        if (writer) A.ctl[mi] = c.done || (global_ns() - t_launch > A.budget_ns);
-        cl.sync();
-        if (threadIdx.x == 0) c.stop = ((volatile int*)A.ctl)[mi];
+        // stop decision of rank 0 (completion or the launch's wall-clock budget), read by the other
+        // ranks from rank 0's shared memory
+        if (writer) c.stop = c.done || (global_ns() - t_launch > A.budget_ns);
+        if (csize > 1) {
+            cl.sync();
+            if (threadIdx.x == 0 && rank != 0) c.stop = *cl.map_shared_rank(&c.stop, 0);
+        }
         __syncthreads();
         if (c.stop) break;
         const double dt = c.dt;
         for (int s = 1; s < 7; ++s) {
             double* dst = (s == 6) ? un : y;
-            for (int comp = 0; comp < 3; ++comp)
-                for (int i = lo + threadIdx.x; i < hi; i += BS) {
-                    const int g = comp * N + i;
-                    double acc = 0.0;
-                    for (int r = 0; r < s; ++r) acc = fma(e_ta[s][r], kk[r][g], acc);
-                    dst[g] = u[g] + dt * acc;
+            // the three components' FMA chains interleaved (FP64 latency, not throughput, binds here)
+            for (int i = lo + threadIdx.x; i < hi; i += BS) {
+                double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
+                for (int r = 0; r < s; ++r) {
+                    const double a = e_ta[s][r];
+                    acc0 = fma(a, kk[r][i], acc0);
+                    acc1 = fma(a, kk[r][N + i], acc1);
+                    acc2 = fma(a, kk[r][2 * N + i], acc2);
                 }
+                dst[i] = u[i] + dt * acc0;
+                dst[N + i] = u[N + i] + dt * acc1;
+                dst[2 * N + i] = u[2 * N + i] + dt * acc2;
+            }
             ens_rhs<BS>(m, A, S, dst, kk[s], lo, hi, cl);
         }
-        double ss = 0.0;
-        int bad = 0;
-        for (int comp = 0; comp < 3; ++comp)
-            for (int i = lo + threadIdx.x; i < hi; i += BS) {
-                const int g = comp * N + i;
-                double e = 0.0;
+        // error norm: per 32-patch chunk, lane i sums r^2 over the three components, then a fixed
+        // shuffle tree; chunk sums go to the (now unused) stage buffer y and are added up in chunk
+        // order after the cluster barrier, identically in every rank
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const int ch0 = lo / 32;
+        for (int ch = ch0 + warp; ch < (hi + 31) / 32; ch += BS / 32) {
+            const int i = 32 * ch + lane;
+            double ss = 0.0;
+            int bad = 0;
+            if (i < N) {
+                double e[3], r[3];
 #pragma unroll
-                for (int s = 0; s < 7; ++s) e = fma(e_te[s], kk[s][g], e);
-                e *= dt;
-                const double unv = un[g];
-                // ψ = ln θ: an absolute ψ error is a relative θ error, scaled by reltol
-                const double sc = (comp == 1 && m.log_theta) ? A.abstol + A.reltol
-                                                             : A.abstol + A.reltol * fmax(fabs(u[g]), fabs(unv));
-                const double r = e / sc;
-                ss = fma(r, r, ss);
-                bad |= !isfinite(unv);
+                for (int comp = 0; comp < 3; ++comp) e[comp] = 0.0;
+#pragma unroll
+                for (int s = 0; s < 7; ++s)
+#pragma unroll
+                    for (int comp = 0; comp < 3; ++comp) e[comp] = fma(e_te[s], kk[s][comp * N + i], e[comp]);
+#pragma unroll
+                for (int comp = 0; comp < 3; ++comp) {
+                    const int g = comp * N + i;
+                    const double unv = un[g];
+                    // ψ = ln θ: an absolute ψ error is a relative θ error, scaled by reltol
+                    const double sc = (comp == 1 && m.log_theta) ? A.abstol + A.reltol
+                                                                 : A.abstol + A.reltol * fmax(fabs(u[g]), fabs(unv));
+                    r[comp] = (e[comp] * dt) / sc;
+                    bad |= !isfinite(unv);
+                }
+                ss = fma(r[0], r[0], ss);  // components summed in order 0, 1, 2
+                ss = fma(r[1], r[1], ss);
+                ss = fma(r[2], r[2], ss);
             }
-        for (int o = 16; o > 0; o >>= 1) {
-            ss += __shfl_xor_sync(0xffffffffu, ss, o);
-            bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+            for (int o = 16; o > 0; o >>= 1) {
+                ss += __shfl_xor_sync(0xffffffffu, ss, o);
+                bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+            }
+            if (lane == 0) S.part[ch - ch0] = bad ? INFINITY : ss;
         }
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = bad ? INFINITY : ss;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double part = 0.0;
-            for (int w = 0; w < BS / 32; ++w) part += red[w];
-            A.part[mi * 16 + rank] = part;
+        if (csize > 1) cl.sync();
+        else __syncthreads();
+        if (warp == 0) {
+            // chunk ch lives in the shared memory of the rank owning it (chunk ranges as above)
+            double tot = 0.0;
+            int r = 0;
+            int r_lo = 0, r_hi = (int)((long long)nch * 1 / csize);
+            for (int ch = lane; ch < nch; ch += 32) {
+                while (ch >= r_hi) {
+                    ++r;
+                    r_lo = r_hi;
+                    r_hi = (int)((long long)nch * (r + 1) / csize);
+                }
+                const double* src = (csize > 1) ? cl.map_shared_rank(S.part, r) : S.part;
+                tot += src[ch - r_lo];
+            }
+            for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+            red[0] = tot;  // lane 0 below
         }
-        cl.sync();
         if (threadIdx.x == 0) {
-            double tot = 0.0;  // same order in every rank
-            for (int r = 0; r < csize; ++r) tot += ((volatile double*)A.part)[mi * 16 + r];
+            const double tot = red[0];
             double EEst = sqrt(tot / (double)(3 * N));
             if (!isfinite(EEst)) EEst = INFINITY;
             const double beta1 = 0.14, beta2 = 0.08, gam = 0.9, qmin = 0.2, qmax = 10.0;
-            const double q11 = pow(EEst, beta1);
+            // the PI gain factors EEst^β1 and qold^β2 only shape the next dt: FP32 (a serial FP64
+            // pow costs ~3 µs per step on this chip); acceptance uses the FP64 norm EEst itself
+            auto powf_ = [](double x, float e) { return (double)exp2f(e * log2f((float)x)); };
+            const double q11 = powf_(EEst, (float)beta1);
             c.iters += 1;
             double dtn;
             int acc = 0;
             if (EEst <= 1.0) {
-                double q = q11 / pow(c.qold, beta2);
+                double q = q11 / powf_(c.qold, (float)beta2);
                 q = fmax(1.0 / qmax, fmin(1.0 / qmin, q / gam));
                 const double tn = c.t + dt;
                 c.t = (tn >= c.t1) ? c.t1 : tn;
@@ -344,9 +392,19 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
                 }
         }
     }
+    // every rank leaves the loop in the same iteration; none may exit while another can still
+    // read its shared memory (the stop flag just read from rank 0)
+    if (csize > 1) cl.sync();
 }
 
 __global__ void k_ens_theta(EnsArgs A, int to_log);
+
+// FFT work arrays Z (nq x P), spectra X (nxi x H), twiddles (P/2), all float2, then one double
+// per 32-patch chunk for the error norm
+size_t ens_smem_bytes(int nx, int nxi, int P) {
+    return sizeof(float2) * ((size_t)((nxi + 1) / 2) * P + (size_t)nxi * (P / 2 + 1) + P / 2) +
+           sizeof(double) * (((size_t)nx * nxi + 31) / 32);
+}
 
 int ens_prepare_model(EnsModel& m, int nx, int nxi, size_t* smem_bytes) {
     if (nx <= 0 || nxi <= 0 || nx > 4096 || nxi > 64)
@@ -355,7 +413,7 @@ int ens_prepare_model(EnsModel& m, int nx, int nxi, size_t* smem_bytes) {
     m.nx = nx; m.nxi = nxi; m.N = nx * nxi;
     m.P = 2; m.logP = 1;
     while (m.P < 2 * nx - 1) { m.P <<= 1; ++m.logP; }
-    *smem_bytes = sizeof(float) * 2 * ((size_t)((nxi + 1) / 2) * m.P + (size_t)nxi * (m.P / 2 + 1) + m.P / 2);
+    *smem_bytes = ens_smem_bytes(nx, nxi, m.P);
     if (*smem_bytes > 200 * 1024) return fail(GBC_EINVAL, "model exceeds the 200 KB shared-memory budget of its FFT buffers");
     return 0;
 }
@@ -370,17 +428,26 @@ int ens_ghat(const double* st_dev, const EnsModel& m, float* ghat_dev, cudaStrea
     return 0;
 }
 
-int ens_csize(int N, int maxc) {
-    const int c = N <= 600 ? 1 : N <= 1200 ? 2 : N <= 2400 ? 4 : 8;
+int ens_csize(int N, int maxc, int boost) {
+    int c = N <= 600 ? 1 : N <= 1200 ? 2 : N <= 2400 ? 4 : 8;
+    if (c < boost) c = boost;
     return c < maxc ? c : maxc;
 }
 
-void ens_groups(const EnsModel* models, int n, int maxc, std::vector<int>& order, int first[4], int count[4]) {
+int ens_boost(int nactive) {
+    int b = 1;
+    while (b < 8 && (long long)nactive * b * 2 <= sm_count()) b *= 2;
+    return b;
+}
+
+// the models still running, grouped by cluster size
+void ens_groups(const EnsModel* models, int n, int maxc, int boost, std::vector<int>& order, int first[4],
+                int count[4]) {
     order.clear();
     for (int g = 0; g < 4; ++g) {
         first[g] = (int)order.size();
         for (int i = 0; i < n; ++i)
-            if (ens_csize(models[i].N, maxc) == (1 << g)) order.push_back(i);
+            if (!models[i].done && ens_csize(models[i].N, maxc, boost) == (1 << g)) order.push_back(i);
         count[g] = (int)order.size() - first[g];
     }
 }
@@ -407,7 +474,7 @@ static int launch_cluster(const EnsArgs& A, int nmod, int csize, size_t smem, cu
 int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtmax, double dtmin,
                    unsigned long long budget_ns, int block, size_t smem, cudaStream_t main) {
     EnsArgs A{};
-    A.models = L.models; A.nmodels = L.n; A.order = L.order; A.part = L.part; A.ctl = L.ctl;
+    A.models = L.models; A.nmodels = L.n; A.order = L.order; A.ctl = L.ctl;
     A.reltol = reltol; A.abstol = abstol; A.dtmax = dtmax; A.dtmin = dtmin;
     A.budget = 1 << 20;
     A.budget_ns = budget_ns;
@@ -438,7 +505,6 @@ int ens_launch_create(EnsLaunch& L, int capacity) {
     L = EnsLaunch();
     L.cap = capacity;
     GBC_CUDA(cudaMalloc(&L.order, sizeof(int) * capacity));
-    GBC_CUDA(cudaMalloc(&L.part, sizeof(double) * 16 * capacity));
     GBC_CUDA(cudaMalloc(&L.ctl, sizeof(int) * capacity));
     GBC_CUDA(cudaEventCreateWithFlags(&L.fork, cudaEventDisableTiming));
     for (int g = 0; g < 4; ++g) {
@@ -450,7 +516,6 @@ int ens_launch_create(EnsLaunch& L, int capacity) {
 
 void ens_launch_destroy(EnsLaunch& L) {
     if (L.order) cudaFree((void*)L.order);
-    if (L.part) cudaFree(L.part);
     if (L.ctl) cudaFree(L.ctl);
     if (L.fork) cudaEventDestroy(L.fork);
     for (int g = 0; g < 4; ++g) {
@@ -461,13 +526,15 @@ void ens_launch_destroy(EnsLaunch& L) {
 }
 
 // uploads the grouped order of the models (host descriptors) and fills the group table
-int ens_launch_prepare(EnsLaunch& L, EnsModel* d_models, const EnsModel* host, int n, int maxc, cudaStream_t s) {
+int ens_launch_prepare(EnsLaunch& L, EnsModel* d_models, const EnsModel* host, int n, int maxc, int boost,
+                       cudaStream_t s) {
     if (n > L.cap) return fail(GBC_EINVAL, "ensemble launch capacity exceeded");
     std::vector<int> order;
-    ens_groups(host, n, maxc, order, L.first, L.count);
+    ens_groups(host, n, maxc, boost, order, L.first, L.count);
     L.models = d_models;
     L.n = n;
-    GBC_CUDA(cudaMemcpyAsync((void*)L.order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    if (!order.empty())
+        GBC_CUDA(cudaMemcpyAsync((void*)L.order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice, s));
     GBC_CUDA(cudaStreamSynchronize(s));
     return 0;
 }
@@ -505,6 +572,7 @@ struct gbc_ensemble {
     double* k[7] = {};
     int block = 256;
     int max_cluster = 8;
+    int regroup = 1;
     int log_theta = 1;
     cudaGraphExec_t exec = nullptr;
     int exec_block = 0, exec_budget = 0;
@@ -580,7 +648,7 @@ int gbc_ensemble_create(int nmodels, const int* nx, const int* nxi, gbc_ensemble
         m.off_n = on; m.off_st = os;
         on += m.N;
         os += (long long)nxi[i] * nxi[i] * (m.P / 2 + 1);
-        const size_t sm = sizeof(float) * 2 * ((size_t)((nxi[i] + 1) / 2) * m.P + (size_t)nxi[i] * (m.P / 2 + 1) + m.P / 2);
+        const size_t sm = ens_smem_bytes(nx[i], nxi[i], m.P);
         e->smem = std::max(e->smem, sm);
     }
     e->total_n = on;
@@ -737,6 +805,12 @@ int gbc_ensemble_set_max_cluster(gbc_ensemble* e, int ctas) {
     return 0;
 }
 
+int gbc_ensemble_set_regroup(gbc_ensemble* e, int on) {
+    if (!e) return fail(GBC_EINVAL, "null ensemble");
+    e->regroup = on != 0;
+    return 0;
+}
+
 int gbc_ensemble_set_log_theta(gbc_ensemble* e, int on) {
     if (!e) return fail(GBC_EINVAL, "null ensemble");
     e->log_theta = on ? 1 : 0;
@@ -770,35 +844,49 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
     cudaStream_t s = e->stream;
     GBC_CUDA(cudaMemcpyAsync(e->d_models, e->host.data(), sizeof(EnsModel) * e->n, cudaMemcpyHostToDevice, s));
     if (u_dev != e->u) GBC_CUDA(cudaMemcpyAsync(e->u, u_dev, sizeof(double) * 3 * e->total_n, cudaMemcpyDeviceToDevice, s));
-    if (int rc = ens_launch_prepare(e->lp, e->d_models, e->host.data(), e->n, e->max_cluster, s)) return rc;
     if (e->log_theta) {
         if (int rc = ens_theta(e->d_models, e->n, 1, s)) return rc;
         count_launches(1);
     }
-    // a captured group of persistent launches (one per cluster size, on forked streams), relaunched
-    // until every model reports done
-    const int group = 4;
-    if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
-    {
+    // A captured pair of persistent launches (one per cluster size, on forked streams, 100 ms of
+    // wall clock each), relaunched until every model reports done. As models finish, the ones
+    // still running move to larger clusters (their FP64 friction, stage and error-norm work spreads
+    // over more SMs; the trajectory does not depend on the cluster size) and the graph is captured
+    // again for the new grouping.
+    auto capture = [&](int boost) -> int {
+        if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
+        if (int rc = ens_launch_prepare(e->lp, e->d_models, e->host.data(), e->n, e->max_cluster, boost, s)) return rc;
         cudaGraph_t g;
         GBC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         int rc = 0;
-        for (int k = 0; k < group && !rc; ++k)
-            rc = ens_run_groups(e->lp, o->reltol, o->abstol, o->dtmax, o->dtmin, 250000000ull, e->block, e->smem, s);
+        for (int k = 0; k < 2 && !rc; ++k)
+            rc = ens_run_groups(e->lp, o->reltol, o->abstol, o->dtmax, o->dtmin, 100000000ull, e->block, e->smem, s);
         cudaError_t ce = cudaStreamEndCapture(s, &g);
         if (rc) return rc;
         GBC_CUDA(ce);
         GBC_CUDA(cudaGraphInstantiate(&e->exec, g, 0));
         cudaGraphDestroy(g);
         e->exec_block = e->block;
-    }
+        return 0;
+    };
+    auto active = [&]() {
+        int a = 0;
+        for (int i = 0; i < e->n; ++i) a += (e->host[i].done == 0);
+        return a;
+    };
+    int boost = e->regroup ? ens_boost(active()) : 1;
+    if (int rc = capture(boost)) return rc;
     for (;;) {
         GBC_CUDA(cudaGraphLaunch(e->exec, s));
         GBC_CUDA(cudaMemcpyAsync(e->host.data(), e->d_models, sizeof(EnsModel) * e->n, cudaMemcpyDeviceToHost, s));
         GBC_CUDA(cudaStreamSynchronize(s));
-        bool all = true;
-        for (int i = 0; i < e->n; ++i) all &= (e->host[i].done != 0);
-        if (all) break;
+        const int na = active();
+        if (na == 0) break;
+        const int nb = e->regroup ? ens_boost(na) : 1;
+        if (nb != boost) {
+            boost = nb;
+            if (int rc = capture(boost)) return rc;
+        }
     }
     if (e->log_theta) {
         if (int rc = ens_theta(e->d_models, e->n, 0, s)) return rc;

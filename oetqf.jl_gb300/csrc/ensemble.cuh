@@ -31,7 +31,6 @@ struct EnsArgs {
     int nmodels;
     const int* order;            // models of this launch, grouped by cluster size: order[first + i]
     int first;
-    double* part;                // per model x 16 cluster ranks: error-norm partial sums
     int* ctl;                    // per model: stop flag of the current step (written by rank 0)
     double reltol, abstol, dtmax, dtmin;
     int budget;                      // step cap per launch and model
@@ -50,16 +49,20 @@ struct EnsLaunch {
     EnsModel* models = nullptr;
     int n = 0, cap = 0;
     const int* order = nullptr;  // device: model indices grouped by cluster size
-    double* part = nullptr;      // device: error-norm partials, 16 per model
     int* ctl = nullptr;          // device: stop flags, one per model
     int first[4] = {0, 0, 0, 0}, count[4] = {0, 0, 0, 0};
     cudaStream_t aux[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t fork = nullptr, join[4] = {nullptr, nullptr, nullptr, nullptr};
 };
-int ens_csize(int N, int maxc);
+// cluster size of a model of N patches: by size, at least `boost`, at most maxc
+int ens_csize(int N, int maxc, int boost);
+// the cluster size every model may use when nactive models share the SMs (1, 2, 4 or 8)
+int ens_boost(int nactive);
 int ens_launch_create(EnsLaunch& L, int capacity);
 void ens_launch_destroy(EnsLaunch& L);
-int ens_launch_prepare(EnsLaunch& L, EnsModel* d_models, const EnsModel* host, int n, int maxc, cudaStream_t s);
+// groups the models of `host` that are not done (uploads their order)
+int ens_launch_prepare(EnsLaunch& L, EnsModel* d_models, const EnsModel* host, int n, int maxc, int boost,
+                       cudaStream_t s);
 // one persistent launch per group: each model runs until done or budget_ns of wall clock
 int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtmax, double dtmin,
                    unsigned long long budget_ns, int block, size_t smem, cudaStream_t main);

@@ -416,7 +416,7 @@ static void scheduler(gbc_server* s) {
             if (!rc) rc = ens_launch_create(s->lp, s->d_desc_cap);
         }
         if (!rc && cudaMemcpyAsync(s->d_desc, h.data(), sizeof(EnsModel) * n, cudaMemcpyHostToDevice, s->batch) != cudaSuccess) rc = GBC_ECUDA;
-        if (!rc) rc = ens_launch_prepare(s->lp, s->d_desc, h.data(), n, 8, s->batch);
+        if (!rc) rc = ens_launch_prepare(s->lp, s->d_desc, h.data(), n, 8, ens_boost(n), s->batch);
         if (!rc) rc = ens_run_groups(s->lp, s->batch_opts.reltol, s->batch_opts.abstol, s->batch_opts.dtmax,
                                      s->batch_opts.dtmin, s->slice_ns, s->block, smem, s->batch);
         if (!rc && cudaMemcpyAsync(h.data(), s->d_desc, sizeof(EnsModel) * n, cudaMemcpyDeviceToHost, s->batch) != cudaSuccess) rc = GBC_ECUDA;

@@ -83,6 +83,7 @@ def lib():
             "gbc_ensemble_set_block": [P, I],
             "gbc_ensemble_set_log_theta": [P, I],
             "gbc_ensemble_set_max_cluster": [P, I],
+            "gbc_ensemble_set_regroup": [P, I],
             "gbc_ensemble_integrate": [P, PD, PD, PD, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
             "gbc_ensemble_integrate_dev": [P, P, PD, PD, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
         }

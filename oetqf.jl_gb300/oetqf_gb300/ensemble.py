@@ -70,6 +70,10 @@ class Ensemble:
     def set_max_cluster(self, ctas: int):
         C.check(C.lib().gbc_ensemble_set_max_cluster(self.h, ctas))
 
+    def set_regroup(self, on: bool):
+        """Move the models still running to larger clusters as others finish (default on)."""
+        C.check(C.lib().gbc_ensemble_set_regroup(self.h, int(bool(on))))
+
     def set_log_theta(self, on: bool):
         C.check(C.lib().gbc_ensemble_set_log_theta(self.h, int(bool(on))))
 

@@ -58,8 +58,8 @@ def test_per_model_horizons_and_blocks():
         assert [s.t for s in st] == list(t1)
         outs[b] = u
     np.testing.assert_array_equal(outs[128][e.offsets[3]:e.offsets[4]], u0[e.offsets[3]:e.offsets[4]])
-    for b in (256, 512):  # CTA size changes reduction order only
-        np.testing.assert_allclose(outs[b], outs[128], rtol=1e-6, atol=1e-12)
+    for b in (256, 512):  # the error norm is summed in a fixed order whatever the CTA size
+        np.testing.assert_array_equal(outs[b], outs[128])
 
 
 def test_cluster_split_models(oracle):
@@ -73,7 +73,7 @@ def test_cluster_split_models(oracle):
     e.set_max_cluster(1)
     u1, st1 = e.integrate(u0, 0.0, T, reltol=1e-8, abstol=1e-10, dt=1e-3)
     assert all(s.status == 0 for s in st8 + st1)
-    np.testing.assert_allclose(u8, u1, rtol=1e-7, atol=1e-15)  # error-norm reduction order differs
+    np.testing.assert_array_equal(u8, u1)  # the trajectory does not depend on the cluster size
     for i in (0, 3):
         m = models[i]
         gf = oracle.gf_ff(m.mf, m.lam, m.mu, fourier=True)
@@ -81,3 +81,18 @@ def test_cluster_split_models(oracle):
         N = m.N
         ui = u8[e.offsets[i]:e.offsets[i] + 3 * N]
         assert np.abs(ui[:N] - uc[:N]).max() / np.abs(uc[:N]).max() < 1e-4
+
+
+def test_regrouping_keeps_trajectories():
+    """Models with staggered horizons: as they finish, the rest move to larger clusters (2, 4, 8
+    CTAs); every state is bitwise the same as without regrouping."""
+    models = fault_ensemble(n_models=40, n_range=(100, 700), seed=31)
+    e, u0 = _build(models)
+    t1 = np.linspace(0.05, 1.5, len(models)) * YEAR
+    e.set_regroup(False)
+    ua, sa = e.integrate(u0, 0.0, t1)
+    e.set_regroup(True)
+    ub, sb = e.integrate(u0, 0.0, t1)
+    assert [s.t for s in sb] == list(t1)
+    assert [s.naccept for s in sa] == [s.naccept for s in sb]
+    np.testing.assert_array_equal(ua, ub)
