@@ -298,6 +298,55 @@ __global__ void __launch_bounds__(256) k_fault_rows_mixed(RhsArgs a, const doubl
     }
 }
 
+// Fault rows through shared memory: one CTA per (16 along-strike patches ii0..ii0+15, depth row j).
+// The CTA stages x = v - vpl for the whole fault and the Toeplitz columns st32[:, j, l] for every
+// source row l (2 N floats); thread (ii, t) sums over source rows l ≡ t (mod 16) and all k, the 16
+// partials of a patch are added in order t = 0..15, and the patch's FP64 friction follows.
+constexpr int kFR_II = 16, kFR_L = 16;
+__global__ void __launch_bounds__(kFR_II * kFR_L) k_fault_rows_smem(RhsArgs a, const double* __restrict__ u,
+                                                                 double* __restrict__ du, StateLayout L) {
+    if (a.skip && *a.skip) return;
+    extern __shared__ float fsm[];
+    const int nx = a.nx, nxi = a.nxi, N = a.N;
+    float* xs = fsm;           // N: x[k + nx l]
+    float* ts = fsm + N;       // nx * nxi: st32[d + nx (j + nxi l)] for this j, as ts[d + nx l]
+    __shared__ float part[kFR_L][kFR_II + 1];
+    const int nb = (nx + kFR_II - 1) / kFR_II;
+    const int j = blockIdx.x / nb, ii0 = (blockIdx.x % nb) * kFR_II;
+    for (int t = threadIdx.x; t < N; t += blockDim.x) xs[t] = (float)(u[L.v + t] - a.vpl);
+    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+        const int d = t % nx, l = t / nx;
+        ts[t] = a.st32[d + (size_t)nx * (j + (size_t)nxi * l)];
+    }
+    __syncthreads();
+    const int il = threadIdx.x % kFR_II, tl = threadIdx.x / kFR_II;
+    const int ii = ii0 + il;
+    float acc = 0.f;
+    if (ii < nx)
+        for (int l = tl; l < nxi; l += kFR_L) {
+            const float* x = xs + nx * l;
+            const float* tt = ts + nx * l;
+            float a0 = 0.f, a1 = 0.f;
+            int k = 0;
+            for (; k + 1 < nx; k += 2) {
+                a0 = fmaf(tt[ii > k ? ii - k : k - ii], x[k], a0);
+                a1 = fmaf(tt[ii > k + 1 ? ii - k - 1 : k + 1 - ii], x[k + 1], a1);
+            }
+            if (k < nx) a0 = fmaf(tt[ii > k ? ii - k : k - ii], x[k], a0);
+            acc += a0 + a1;
+        }
+    part[tl][il] = acc;
+    __syncthreads();
+    if (tl == 0 && ii < nx) {
+        float s = 0.f;
+        for (int t = 0; t < kFR_L; ++t) s += part[t][il];
+        const int i = ii + nx * j;
+        fault_friction(a, u, du, L, i, (double)s + (a.ne > 0 ? (double)a.y32[i] : 0.0));
+    }
+}
+
+size_t fault_rows_smem_bytes(int N, int nx, int nxi) { return sizeof(float) * ((size_t)N + (size_t)nx * nxi); }
+
 int launch_rhs_mixed(const RhsArgs& a, const double* u, double* du, cudaStream_t s) {
     const StateLayout L = layout_of(a.N, a.ne);
     const int sms = sm_count();
@@ -333,9 +382,20 @@ int launch_rhs_mixed(const RhsArgs& a, const double* u, double* du, cudaStream_t
         }
         GBC_CUDA(cudaGetLastError());
     }
-    int g = (a.N + 7) / 8;
-    if (g > sms * 8) g = sms * 8;
-    k_fault_rows_mixed<<<g, 256, 0, s>>>(a, u, du, L);
+    const size_t fsm = fault_rows_smem_bytes(a.N, a.nx, a.nxi);
+    if (fsm <= 160 * 1024) {
+        static bool attr = false;
+        if (!attr) {
+            GBC_CUDA(cudaFuncSetAttribute(k_fault_rows_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+            attr = true;
+        }
+        const int nb = (a.nx + kFR_II - 1) / kFR_II;
+        k_fault_rows_smem<<<nb * a.nxi, kFR_II * kFR_L, fsm, s>>>(a, u, du, L);
+    } else {  // faults above ~20k patches: one warp per row through L2
+        int g = (a.N + 7) / 8;
+        if (g > sms * 8) g = sms * 8;
+        k_fault_rows_mixed<<<g, 256, 0, s>>>(a, u, du, L);
+    }
     GBC_CUDA(cudaGetLastError());
     return 0;
 }
