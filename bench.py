@@ -525,6 +525,8 @@ def run_serving(args):
                                                      "batch_iterations": info.iterations, "makespan_s": out["makespan_s"]},
                       out["makespan_s"] * 1e3 / len(reqs), "f32+f64 / bf16")
     line["latency_s"] = {"p50": out["p50_s"], "p99": out["p99_s"], "max": float(lat.max())}
+    line["gf_cache"] = {"hits": info.cache_hits, "misses": info.cache_misses, "resident_entries": info.cache_entries,
+                        "resident_bytes": info.cache_bytes}
     line["status"] = out["status"]
     print(json.dumps(line), flush=True)
 
