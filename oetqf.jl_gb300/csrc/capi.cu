@@ -5,7 +5,10 @@
 #include <algorithm>
 #include <atomic>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "gbc_internal.cuh"
@@ -23,6 +26,19 @@ int fail(int code, const std::string& msg) {
 int cuda_fail(cudaError_t e, const char* what) {
     g_err = std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e);
     return (e == cudaErrorMemoryAllocation) ? GBC_ENOMEM : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? GBC_ENODEV : GBC_ECUDA;
+}
+
+int set_smem_limit(const void* fn, int bytes) {
+    int dev = 0;
+    GBC_CUDA(cudaGetDevice(&dev));
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, int> done;  // (kernel, device) -> limit set
+    std::lock_guard<std::mutex> lk(mu);
+    int& have = done[std::make_pair(fn, dev)];
+    if (have >= bytes) return 0;
+    GBC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    have = bytes;
+    return 0;
 }
 
 int sm_count() {

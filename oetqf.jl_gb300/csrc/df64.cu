@@ -215,11 +215,7 @@ __global__ void __launch_bounds__(kDThreads, kDCtasPerSM) k_gemv_df64(const __gr
 
 int launch_gemv_df64(const RhsArgs& a, const double* u, double* du, cudaStream_t s) {
     const size_t smem = df64_smem_bytes();
-    static bool attr = false;
-    if (!attr) {
-        GBC_CUDA(cudaFuncSetAttribute(k_gemv_df64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = true;
-    }
+    if (int rc = set_smem_limit((const void*)k_gemv_df64, (int)smem)) return rc;
     const int ntiles = (int)(a.rowsq / DR);
     const int slots = sm_count() * kDCtasPerSM;
     const int grid = ntiles < slots ? ntiles : slots;

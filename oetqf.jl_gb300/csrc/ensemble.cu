@@ -454,7 +454,7 @@ void ens_groups(const EnsModel* models, int n, int maxc, int boost, std::vector<
 
 template <int BS>
 static int launch_cluster(const EnsArgs& A, int nmod, int csize, size_t smem, cudaStream_t s) {
-    GBC_CUDA(cudaFuncSetAttribute(k_ensemble<BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (int rc = set_smem_limit((const void*)k_ensemble<BS>, (int)smem)) return rc;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(nmod * csize));
     cfg.blockDim = dim3(BS);

@@ -22,6 +22,9 @@ int cuda_fail(cudaError_t e, const char* what);
 
 constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs (grids are sized from the live count)
 int sm_count();
+// raises a kernel's dynamic shared-memory limit on the current device (the attribute is per
+// device; thread-safe, set once per kernel, device and size)
+int set_smem_limit(const void* fn, int bytes);
 
 // Gauss-Legendre tables for the strain-volume stacks (4, 8, 12, 16 nodes), in constant memory.
 void gl_rule(int n, double* x, double* w);

@@ -8,6 +8,8 @@
 // stack of Okada dislocation planes through the cuboid integrated over its thickness with
 // Gauss-Legendre panels: a uniform eigenstrain eps* equals a continuous stack of dislocations
 // with sym(b (x) n) = eps* per unit thickness.
+#include <mutex>
+#include <set>
 #include <cuda_runtime.h>
 
 #include "gbc_internal.cuh"
@@ -45,17 +47,20 @@ void gl_rule(int n, double* x, double* w) {
     }
 }
 
+// constant memory is per device: the tables are uploaded once for each device that assembles
 int upload_gl_tables() {
-    static int done = -1;
+    static std::mutex mu;
+    static std::set<int> done;
     int dev = 0;
     GBC_CUDA(cudaGetDevice(&dev));
-    if (done == dev) return 0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count(dev)) return 0;
     double x[4][16] = {{0}}, w[4][16] = {{0}};
     const int ord[4] = {4, 8, 12, 16};
     for (int k = 0; k < 4; ++k) gl_rule(ord[k], x[k], w[k]);
     GBC_CUDA(cudaMemcpyToSymbol(c_glx, x, sizeof(x)));
     GBC_CUDA(cudaMemcpyToSymbol(c_glw, w, sizeof(w)));
-    done = dev;
+    done.insert(dev);
     return 0;
 }
 

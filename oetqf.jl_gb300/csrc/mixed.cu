@@ -366,29 +366,17 @@ int launch_rhs_mixed(const RhsArgs& a, const double* u, double* du, cudaStream_t
         CUtensorMap tm;
         memcpy(&tm, a.tmap, sizeof(tm));
         if (a.mode == GBC_PREC_BF16) {
-            static bool attr = false;
-            if (!attr) {
-                GBC_CUDA(cudaFuncSetAttribute(k_gemv_tma<GBC_PREC_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-                attr = true;
-            }
+            if (int rc = set_smem_limit((const void*)k_gemv_tma<GBC_PREC_BF16>, (int)smem)) return rc;
             k_gemv_tma<GBC_PREC_BF16><<<grid, 256, smem, s>>>(tm, a, du + L.sig);
         } else {
-            static bool attr = false;
-            if (!attr) {
-                GBC_CUDA(cudaFuncSetAttribute(k_gemv_tma<GBC_PREC_F16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-                attr = true;
-            }
+            if (int rc = set_smem_limit((const void*)k_gemv_tma<GBC_PREC_F16>, (int)smem)) return rc;
             k_gemv_tma<GBC_PREC_F16><<<grid, 256, smem, s>>>(tm, a, du + L.sig);
         }
         GBC_CUDA(cudaGetLastError());
     }
     const size_t fsm = fault_rows_smem_bytes(a.N, a.nx, a.nxi);
     if (fsm <= 160 * 1024) {
-        static bool attr = false;
-        if (!attr) {
-            GBC_CUDA(cudaFuncSetAttribute(k_fault_rows_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
-            attr = true;
-        }
+        if (int rc = set_smem_limit((const void*)k_fault_rows_smem, 160 * 1024)) return rc;
         const int nb = (a.nx + kFR_II - 1) / kFR_II;
         k_fault_rows_smem<<<nb * a.nxi, kFR_II * kFR_L, fsm, s>>>(a, u, du, L);
     } else {  // faults above ~20k patches: one warp per row through L2
