@@ -483,6 +483,7 @@ def run_ensemble(args):
                                        "patch_range": [int(min(mm.N for mm in models)), int(max(mm.N for mm in models))],
                                        "horizon_yr": years, "cta_threads": best, "autotune_s": tim,
                                        "rk_steps_min_mean_max": [int(steps.min()), float(steps.mean()), int(steps.max())],
+                                       "slowest_member_patches": int(models[int(np.argmax(steps))].N),
                                        "precision": "FP32 rFFT convolution in shared memory; FP64 friction, ln-theta state, stages, error norm (PI gain factors in FP32)",
                                        "regroup": "models still running move to 2/4/8-CTA clusters as others finish",
                                        "l2": "state and spectra L2-resident (per-model working set)"}, ms, "f32+f64")
