@@ -19,6 +19,7 @@
 
 #include "ensemble.cuh"
 #include "gbc_internal.cuh"
+#include "tma.cuh"
 
 namespace gbc {
 
@@ -46,8 +47,41 @@ struct EnsSmem {
     float2* Z;
     float2* X;
     float2* tw;
-    double* part;  // error-norm sums of this rank's 32-patch chunks
+    double* pr;     // 2 x (nch + 1): error-norm sums of every 32-patch chunk + rank 0's stop flag
+    uint64_t* mb;   // mbarriers: received slip rates (buffers 0, 1), received norms (2, 3)
+    float* xr;      // 2 x N: v - vpl of every patch (clusters: own slice + the peers' pushes)
 };
+
+// ---- cluster exchange: st.async pushes into the peers' shared memory, completing a transaction
+// count on the peer's mbarrier (no cluster-wide release fence over the global stores) -------------
+__device__ __forceinline__ unsigned peer_addr(const void* p, int rank) {
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void push_f32(const float* dst, float v, const uint64_t* bar, int rank) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(peer_addr(dst, rank)),
+                 "r"(__float_as_uint(v)), "r"(peer_addr(bar, rank))
+                 : "memory");
+}
+__device__ __forceinline__ void push_f64(const double* dst, double v, const uint64_t* bar, int rank) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(peer_addr(dst, rank)),
+                 "l"(__double_as_longlong(v)), "r"(peer_addr(bar, rank))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, unsigned parity) {
+    for (long long i = 0; i < kWaitLimit; ++i) {
+        unsigned ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 
@@ -108,15 +142,13 @@ __device__ __forceinline__ void fft_many(float2* Z, int nq, int P, int logP, con
 // of the reference (equation.jl:44-61) done in shared memory: two real rows per complex FFT,
 // a real per-frequency mixing (the symmetric circulant kernel has a real spectrum), two output
 // rows per inverse FFT.
+// xin: v - vpl of every patch in shared memory (cluster ranks, after the exchange), or null to
+// read the stage state y itself (one-CTA models).
 template <int BS>
 __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, const EnsSmem& S,
                                         const double* __restrict__ y, double* __restrict__ k, int lo, int hi,
-                                        cooperative_groups::cluster_group& cl) {
-    // every rank's slice of y (the stage state) must be visible before the full slip-rate vector is
-    // read; a one-CTA model only needs its own writes, which a CTA barrier orders without the
-    // cluster barrier's release/acquire fence
-    if (cl.num_blocks() > 1) cl.sync();
-    else __syncthreads();
+                                        const float* xin) {
+    __syncthreads();
     const int N = m.N, nx = m.nx, nxi = m.nxi, P = m.P, logP = m.logP, H = P / 2 + 1;
     const int nq = (nxi + 1) / 2;
     const double* v = y;
@@ -126,8 +158,13 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
         const int q = t / P, i = t - q * P;
         float re = 0.f, im = 0.f;
         if (i < nx) {
-            re = (float)(v[i + nx * (2 * q)] - m.vpl);
-            if (2 * q + 1 < nxi) im = (float)(v[i + nx * (2 * q + 1)] - m.vpl);
+            if (xin) {
+                re = xin[i + nx * (2 * q)];
+                if (2 * q + 1 < nxi) im = xin[i + nx * (2 * q + 1)];
+            } else {
+                re = (float)(v[i + nx * (2 * q)] - m.vpl);
+                if (2 * q + 1 < nxi) im = (float)(v[i + nx * (2 * q + 1)] - m.vpl);
+            }
         }
         S.Z[q * P + (__brev(i) >> (32 - logP))] = make_float2(re, im);
     }
@@ -232,47 +269,75 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
     const int lo = 32 * (int)((long long)nch * rank / csize);
     const int hi = min(N, 32 * (int)((long long)nch * (rank + 1) / csize));
     const int nq = (m.nxi + 1) / 2, H = m.P / 2 + 1;
+    const int c0 = (int)((long long)nch * rank / csize), c1 = (int)((long long)nch * (rank + 1) / csize);
+    const bool clus = csize > 1;
     EnsSmem S;
     S.Z = reinterpret_cast<float2*>(sm);
     S.X = S.Z + (size_t)nq * m.P;
     S.tw = S.X + (size_t)m.nxi * H;
-    S.part = reinterpret_cast<double*>(S.tw + m.P / 2);
+    S.pr = reinterpret_cast<double*>(S.tw + m.P / 2);
+    S.mb = reinterpret_cast<uint64_t*>(S.pr + 2 * (nch + 1));
+    S.xr = reinterpret_cast<float*>(S.mb + 4);
     for (int t = threadIdx.x; t < m.P / 2; t += BS) {
         double sn, cs;
         sincospi(2.0 * t / m.P, &sn, &cs);
         S.tw[t] = make_float2((float)cs, (float)-sn);
     }
+    __shared__ int xfail;  // a bounded exchange wait gave up
     if (threadIdx.x == 0) {
         c.t = m.t; c.dt = m.dt; c.t1 = m.t1; c.qold = m.qold;
         c.naccept = m.naccept; c.nreject = m.nreject; c.iters = m.iters; c.maxiters = m.maxiters;
         c.done = m.done; c.status = m.status; c.go = 0; c.stop = 0;
+        xfail = 0;
+        if (clus) {
+            for (int b = 0; b < 4; ++b) mbar_init(&S.mb[b], 1);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
     }
-    __syncthreads();
+    if (clus) cl.sync();  // every peer's barriers exist before the first push
+    else __syncthreads();
     double* u = m.u;
     double* kk[7];
     for (int s = 0; s < 7; ++s) kk[s] = m.k[s];
     double* y = m.y;
     double* un = m.un;
     const bool writer = (rank == 0 && threadIdx.x == 0);
-    if (!m.started) {  // FSAL seed
-        ens_rhs<BS>(m, A, S, u, kk[0], lo, hi, cl);
-        if (writer) M.started = 1;
-    }
-    for (int step = 0; step < A.budget; ++step) {
-        // stop decision of rank 0 (completion or the launch's wall-clock budget), shared through L2
-        // stop decision of rank 0 (completion or the launch's wall-clock budget), read by the other
-        // ranks from rank 0's shared memory
-        if (writer) c.stop = c.done || (global_ns() - t_launch > A.budget_ns);
-        if (csize > 1) {
-            cl.sync();
-            if (threadIdx.x == 0 && rank != 0) c.stop = *cl.map_shared_rank(&c.stop, 0);
+    // thread 0's parity of the current phase of each exchange barrier (bit b; a phase per use)
+    unsigned phase = 0;
+    auto collect = [&](int b, unsigned bytes) {
+        if (threadIdx.x == 0) {
+            mbar_expect_tx(&S.mb[b], bytes);  // the peers' bytes of this phase (some may be in already)
+            if (!mbar_wait_cluster(&S.mb[b], (phase >> b) & 1u)) xfail = 1;
+            phase ^= 1u << b;
         }
         __syncthreads();
-        if (c.stop) break;
+    };
+    const unsigned xbytes = 4u * (unsigned)(N - (hi - lo));
+    int rx = 0;  // RHS evaluations in this launch: slip-rate buffer rx & 1
+    if (!m.started) {  // FSAL seed
+        const float* xin = nullptr;
+        if (clus) {
+            float* xb = S.xr + (size_t)(rx & 1) * N;
+            for (int i = lo + threadIdx.x; i < hi; i += BS) {
+                const float x = (float)(u[i] - m.vpl);
+                xb[i] = x;
+                for (int d = 1; d < csize; ++d) push_f32(xb + i, x, &S.mb[rx & 1], (rank + d) % csize);
+            }
+            collect(rx & 1, xbytes);
+            xin = xb;
+        }
+        if (!xfail) ens_rhs<BS>(m, A, S, u, kk[0], lo, hi, xin);
+        ++rx;
+        if (writer) M.started = 1;
+    }
+    for (int step = 0; step < A.budget && !xfail; ++step) {
+        if (c.stop) break;  // decided by the last step's controller, identically in every rank
         const double dt = c.dt;
         for (int s = 1; s < 7; ++s) {
             double* dst = (s == 6) ? un : y;
-            // the three components' FMA chains interleaved (FP64 latency, not throughput, binds here)
+            float* xb = S.xr + (size_t)(rx & 1) * N;
+            // the three components' FMA chains interleaved (FP64 latency, not throughput, binds here);
+            // cluster ranks publish v - vpl of their slice to every peer as they go
             for (int i = lo + threadIdx.x; i < hi; i += BS) {
                 double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
                 for (int r = 0; r < s; ++r) {
@@ -281,29 +346,42 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
                     acc1 = fma(a, kk[r][N + i], acc1);
                     acc2 = fma(a, kk[r][2 * N + i], acc2);
                 }
-                dst[i] = u[i] + dt * acc0;
+                const double vnew = u[i] + dt * acc0;
+                dst[i] = vnew;
                 dst[N + i] = u[N + i] + dt * acc1;
                 dst[2 * N + i] = u[2 * N + i] + dt * acc2;
+                if (clus) {
+                    const float x = (float)(vnew - m.vpl);
+                    xb[i] = x;
+                    for (int d = 1; d < csize; ++d) push_f32(xb + i, x, &S.mb[rx & 1], (rank + d) % csize);
+                }
             }
-            ens_rhs<BS>(m, A, S, dst, kk[s], lo, hi, cl);
+            if (clus) {
+                collect(rx & 1, xbytes);
+                if (xfail) break;
+            }
+            ens_rhs<BS>(m, A, S, dst, kk[s], lo, hi, clus ? xb : nullptr);
+            ++rx;
         }
+        if (xfail) break;
         // error norm: per 32-patch chunk, lane i sums r^2 over the three components, then a fixed
-        // shuffle tree; chunk sums go to the (now unused) stage buffer y and are added up in chunk
-        // order after the cluster barrier, identically in every rank
+        // shuffle tree; the chunk sums (pushed to every rank) are added in chunk order, identically
+        // in every rank, together with rank 0's wall-clock stop flag
+        const int e = step & 1;
+        double* prb = S.pr + (size_t)e * (nch + 1);
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        const int ch0 = lo / 32;
-        for (int ch = ch0 + warp; ch < (hi + 31) / 32; ch += BS / 32) {
+        for (int ch = c0 + warp; ch < c1; ch += BS / 32) {
             const int i = 32 * ch + lane;
             double ss = 0.0;
             int bad = 0;
             if (i < N) {
-                double e[3], r[3];
+                double ev[3], r[3];
 #pragma unroll
-                for (int comp = 0; comp < 3; ++comp) e[comp] = 0.0;
+                for (int comp = 0; comp < 3; ++comp) ev[comp] = 0.0;
 #pragma unroll
                 for (int s = 0; s < 7; ++s)
 #pragma unroll
-                    for (int comp = 0; comp < 3; ++comp) e[comp] = fma(e_te[s], kk[s][comp * N + i], e[comp]);
+                    for (int comp = 0; comp < 3; ++comp) ev[comp] = fma(e_te[s], kk[s][comp * N + i], ev[comp]);
 #pragma unroll
                 for (int comp = 0; comp < 3; ++comp) {
                     const int g = comp * N + i;
@@ -311,7 +389,7 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
                     // ψ = ln θ: an absolute ψ error is a relative θ error, scaled by reltol
                     const double sc = (comp == 1 && m.log_theta) ? A.abstol + A.reltol
                                                                  : A.abstol + A.reltol * fmax(fabs(u[g]), fabs(unv));
-                    r[comp] = (e[comp] * dt) / sc;
+                    r[comp] = (ev[comp] * dt) / sc;
                     bad |= !isfinite(unv);
                 }
                 ss = fma(r[0], r[0], ss);  // components summed in order 0, 1, 2
@@ -322,24 +400,26 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
                 ss += __shfl_xor_sync(0xffffffffu, ss, o);
                 bad |= __shfl_xor_sync(0xffffffffu, bad, o);
             }
-            if (lane == 0) S.part[ch - ch0] = bad ? INFINITY : ss;
-        }
-        if (csize > 1) cl.sync();
-        else __syncthreads();
-        if (warp == 0) {
-            // chunk ch lives in the shared memory of the rank owning it (chunk ranges as above)
-            double tot = 0.0;
-            int r = 0;
-            int r_lo = 0, r_hi = (int)((long long)nch * 1 / csize);
-            for (int ch = lane; ch < nch; ch += 32) {
-                while (ch >= r_hi) {
-                    ++r;
-                    r_lo = r_hi;
-                    r_hi = (int)((long long)nch * (r + 1) / csize);
-                }
-                const double* src = (csize > 1) ? cl.map_shared_rank(S.part, r) : S.part;
-                tot += src[ch - r_lo];
+            if (lane == 0) {
+                const double val = bad ? INFINITY : ss;
+                prb[ch] = val;
+                for (int d = 1; d < csize; ++d) push_f64(prb + ch, val, &S.mb[2 + e], (rank + d) % csize);
             }
+        }
+        if (writer) {
+            const double f = (global_ns() - t_launch > A.budget_ns) ? 1.0 : 0.0;
+            prb[nch] = f;
+            for (int d = 1; d < csize; ++d) push_f64(prb + nch, f, &S.mb[2 + e], d);
+        }
+        if (clus) {
+            collect(2 + e, 8u * (unsigned)(nch - (c1 - c0)) + (rank != 0 ? 8u : 0u));
+            if (xfail) break;
+        } else {
+            __syncthreads();
+        }
+        if (warp == 0) {
+            double tot = 0.0;
+            for (int ch = lane; ch < nch; ch += 32) tot += prb[ch];
             for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
             red[0] = tot;  // lane 0 below
         }
@@ -350,7 +430,7 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
             const double beta1 = 0.14, beta2 = 0.08, gam = 0.9, qmin = 0.2, qmax = 10.0;
             // the PI gain factors EEst^β1 and qold^β2 only shape the next dt: FP32 (a serial FP64
             // pow costs ~3 µs per step on this chip); acceptance uses the FP64 norm EEst itself
-            auto powf_ = [](double x, float e) { return (double)exp2f(e * log2f((float)x)); };
+            auto powf_ = [](double x, float ex) { return (double)exp2f(ex * log2f((float)x)); };
             const double q11 = powf_(EEst, (float)beta1);
             c.iters += 1;
             double dtn;
@@ -376,6 +456,7 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
             if (dtn >= rem) dtn = rem;
             c.dt = dtn;
             c.go = acc;
+            c.stop = c.done || (prb[nch] != 0.0);
             if (rank == 0) {
                 M.t = c.t; M.dt = c.dt; M.qold = c.qold;
                 M.naccept = c.naccept; M.nreject = c.nreject; M.iters = c.iters;
@@ -392,18 +473,23 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
                 }
         }
     }
-    // every rank leaves the loop in the same iteration; none may exit while another can still
-    // read its shared memory (the stop flag just read from rank 0)
-    if (csize > 1) cl.sync();
+    if (xfail && writer) {  // an exchange timed out: the model stops with an error status
+        M.done = 1;
+        M.status = -6;
+    }
+    // every rank leaves the loop at the same step (or on a timed-out exchange); none may exit
+    // while a peer can still push into its shared memory
+    if (clus) cl.sync();
 }
 
 __global__ void k_ens_theta(EnsArgs A, int to_log);
 
-// FFT work arrays Z (nq x P), spectra X (nxi x H), twiddles (P/2), all float2, then one double
-// per 32-patch chunk for the error norm
+// FFT work arrays Z (nq x P), spectra X (nxi x H), twiddles (P/2), all float2; two buffers of
+// chunk norms + stop flag (doubles); four mbarriers; two slip-rate buffers of N floats
 size_t ens_smem_bytes(int nx, int nxi, int P) {
+    const size_t N = (size_t)nx * nxi, nch = (N + 31) / 32;
     return sizeof(float2) * ((size_t)((nxi + 1) / 2) * P + (size_t)nxi * (P / 2 + 1) + P / 2) +
-           sizeof(double) * (((size_t)nx * nxi + 31) / 32);
+           sizeof(double) * 2 * (nch + 1) + sizeof(uint64_t) * 4 + sizeof(float) * 2 * N;
 }
 
 int ens_prepare_model(EnsModel& m, int nx, int nxi, size_t* smem_bytes) {

@@ -1,6 +1,8 @@
 // mbarrier and bulk-copy helpers shared by the TMA-fed GEMVs (inline PTX, sm_90+ forms).
 // Every wait is bounded by kWaitLimit polls; callers turn a timeout into an error word.
 #pragma once
+#include <cuda.h>
+
 #include <cstdint>
 
 namespace gbc {
