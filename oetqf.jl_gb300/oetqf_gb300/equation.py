@@ -115,9 +115,10 @@ class GB300Model:
                                            lam, mu, _ftype(ftype), nrept, buffer_ratio, k(qc), k(qw), len(qw)))
 
     def save_gf(self, file: str) -> None:
-        """Write this model's Green's functions (gf₁₁ as the complex rFFT form) to a file."""
+        """Write this model's Green's functions to a file; gf₁₁ as the real Toeplitz kernel, which
+        the model holds exactly (the complex rFFT form of the reference also loads)."""
         from .persist import save_greens_functions
-        g = {"gf11": self.export_gf(C.GBC_GF11_DFT)}
+        g = {"gf11": self.export_gf(C.GBC_GF11_REAL)}
         if self.ne:
             g.update(gf12=self.export_gf(C.GBC_GF12), gf21=self.export_gf(C.GBC_GF21), gf22=self.export_gf(C.GBC_GF22))
         save_greens_functions(file, **g)
@@ -126,9 +127,12 @@ class GB300Model:
         """Set this model's Green's functions from a file written by save_gf (no assembly)."""
         from .persist import load_greens_functions
         g = load_greens_functions(file)
-        which = {"gf11": C.GBC_GF11_DFT, "gf12": C.GBC_GF12, "gf21": C.GBC_GF21, "gf22": C.GBC_GF22}
+        which = {"gf12": C.GBC_GF12, "gf21": C.GBC_GF21, "gf22": C.GBC_GF22}
         for k, v in g.items():
-            self.set_gf(which[k], v)
+            if k == "gf11":  # complex: the rFFT form of stress_greens_function(...; fourier=true)
+                self.set_gf(C.GBC_GF11_DFT if np.iscomplexobj(v) else C.GBC_GF11_REAL, v)
+            else:
+                self.set_gf(which[k], v)
 
     def export_gf(self, which: int) -> np.ndarray:
         N, M = self.N, 6 * self.ne
