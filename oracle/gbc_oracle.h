@@ -100,12 +100,14 @@ void orc_ode_visco(const orc_model* m, const double* v, const double* th, const 
 void orc_ode_dilatancy(const orc_model* m, const double* v, const double* th, const double* p,
                        double* dv, double* dth, double* ddelta, double* dp);
 
-/* Adaptive Tsit5 integration of the flattened state in ArrayPartition order.
+/* Adaptive integration of the flattened state in ArrayPartition order: Tsit5 (the reference's
+ * tests) or VCABM5 (the reference's example, examples/otf-with-mantle.jl:160-162).
  * Returns 0 on reaching t1, else a negative status; fills counters. */
 typedef struct {
     double reltol, abstol, dt0, dtmax, dtmin;
     long long maxiters;
     int mantle;                            /* 0: fault-only, 1: viscoelastic, 2: dilatancy state */
+    int alg;                               /* 0: Tsit5, 1: VCABM5 (Adams-Bashforth-Moulton, PECE) */
 } orc_solver_opts;
 typedef struct { long long naccept, nreject, nrhs; double t, dt; int status; } orc_solver_stats;
 int orc_integrate(const orc_model* m, double* u, double t0, double t1, const orc_solver_opts* o,
@@ -117,6 +119,9 @@ int orc_integrate_record(const orc_model* m, double* u, double t0, double t1, co
                          orc_solver_stats* st, int stride, long long max_records, double* t_out,
                          double* u_out, long long* nrec);
 int orc_num_threads(void);
+/* The VCABM step coefficients psi (k), beta (k) and Adams weights g_0..g_k for order k and step h
+ * given psi_prev (the previous step's psi); exposed for tests. */
+void orc_abm_coefficients(int k, double h, const double* psi_prev, double* psi, double* beta, double* g);
 
 #ifdef __cplusplus
 }

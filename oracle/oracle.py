@@ -42,9 +42,12 @@ class Model(ctypes.Structure):
                 ("gf11_dft", PD), ("gf12", PD), ("gf21", PD), ("gf22", PD)]
 
 
+ALGS = {"Tsit5": 0, "VCABM5": 1}
+
+
 class SolverOpts(ctypes.Structure):
     _fields_ = [("reltol", D), ("abstol", D), ("dt0", D), ("dtmax", D), ("dtmin", D),
-                ("maxiters", ctypes.c_longlong), ("mantle", I)]
+                ("maxiters", ctypes.c_longlong), ("mantle", I), ("alg", I)]
 
 
 class SolverStats(ctypes.Structure):
@@ -89,6 +92,8 @@ def lib():
             L.orc_num_threads.restype = I
             L.orc_dtau_dt.argtypes = [ctypes.POINTER(Model), PD, PD]
             L.orc_tsit5_tableau.argtypes = [PD, PD]
+            L.orc_abm_coefficients.argtypes = [I, D, PD, PD, PD, PD]
+            L.orc_abm_coefficients.restype = None
             _lib = L
     return _lib
 
@@ -241,19 +246,22 @@ class OracleModel:
         lib().orc_dtau_dt(ctypes.byref(self.m), _p(v), _p(out))
         return out
 
-    def integrate(self, u0, t0, t1, reltol=1e-6, abstol=1e-8, dt0=1e-8, dtmax=np.inf, dtmin=1e-14, maxiters=10**9):
+    def integrate(self, u0, t0, t1, reltol=1e-6, abstol=1e-8, dt0=1e-8, dtmax=np.inf, dtmin=1e-14, maxiters=10**9,
+                  alg="Tsit5"):
         u = _c(u0).copy()
-        o = SolverOpts(reltol, abstol, dt0, dtmax, dtmin, maxiters, 2 if self.dilatancy else (1 if self.ne else 0))
+        o = SolverOpts(reltol, abstol, dt0, dtmax, dtmin, maxiters, 2 if self.dilatancy else (1 if self.ne else 0),
+                       ALGS[alg])
         s = SolverStats()
         lib().orc_integrate(ctypes.byref(self.m), _p(u), t0, t1, ctypes.byref(o), ctypes.byref(s))
         return u, s
 
 
 def integrate_record(om, u0, t0, t1, stride, max_records, reltol=1e-6, abstol=1e-8, dt0=1e-8, dtmax=np.inf,
-                     dtmin=1e-14, maxiters=10**9):
+                     dtmin=1e-14, maxiters=10**9, alg="Tsit5"):
     """orc_integrate_record: returns (u(t1), stats, t_records, u_records)."""
     u = _c(u0).copy()
-    o = SolverOpts(reltol, abstol, dt0, dtmax, dtmin, maxiters, 2 if om.dilatancy else (1 if om.ne else 0))
+    o = SolverOpts(reltol, abstol, dt0, dtmax, dtmin, maxiters, 2 if om.dilatancy else (1 if om.ne else 0),
+                   ALGS[alg])
     s = SolverStats()
     t_out = np.zeros(max_records)
     u_out = np.zeros(max_records * u.size)
@@ -262,6 +270,15 @@ def integrate_record(om, u0, t0, t1, stride, max_records, reltol=1e-6, abstol=1e
                                max_records, _p(t_out), _p(u_out), ctypes.byref(nrec))
     k = nrec.value
     return u, s, t_out[:k], u_out[:k * u.size].reshape(k, u.size)
+
+
+def abm_coefficients(k, h, psi_prev):
+    """orc_abm_coefficients: (psi[:k], beta[:k], g[:k+1]) of one VCABM step."""
+    pp = np.zeros(5)
+    pp[:len(psi_prev)] = psi_prev
+    psi, beta, g = np.zeros(6), np.zeros(6), np.zeros(7)
+    lib().orc_abm_coefficients(int(k), float(h), _p(pp), _p(psi), _p(beta), _p(g))
+    return psi[:k], beta[:k], g[:k + 1]
 
 
 def tsit5_tableau():

@@ -180,3 +180,70 @@ def test_composite_viscoelastic_rhs(oracle):
     tau = np.sqrt(dev[:, 0]**2 + dev[:, 3]**2 + dev[:, 5]**2 + 2 * (dev[:, 1]**2 + dev[:, 2]**2 + dev[:, 4]**2))
     f = sum(q.γ * tau ** q.n for q in laws)
     np.testing.assert_allclose(du[2 * N:2 * N + 6 * ne], (f[:, None] * dev).reshape(-1, order="F"), rtol=1e-13)
+
+
+# ---- VCABM5 (the reference example's integrator, examples/otf-with-mantle.jl:160-162) -------------
+def test_abm_weights_constant_step(oracle):
+    """Equal steps: beta = 1 and g_j are the Adams-Bashforth backward-difference weights."""
+    h = 0.37
+    psi, beta, g = oracle.abm_coefficients(5, h, [h, 2 * h, 3 * h, 4 * h])
+    np.testing.assert_allclose(psi, [h, 2 * h, 3 * h, 4 * h, 5 * h], rtol=1e-15)
+    np.testing.assert_allclose(beta, np.ones(5), rtol=1e-15)
+    np.testing.assert_allclose(g, [1, 1 / 2, 5 / 12, 3 / 8, 251 / 720, 95 / 288], rtol=1e-14)
+
+
+def _divided(xs, fs):
+    """Newton divided differences f[x0], f[x0,x1], ... of the points in the given order."""
+    c = list(fs)
+    out = [c[0]]
+    for j in range(1, len(xs)):
+        c = [(c[i + 1] - c[i]) / (xs[i + j] - xs[i]) for i in range(len(xs) - j)]
+        out.append(c[0])
+    return out
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5])
+def test_abm_variable_step_is_exact_on_polynomials(oracle, k):
+    """With uneven history, the order-k predictor integrates polynomials of degree < k exactly over
+    the step and the corrector those of degree <= k (Phi from divided differences, HNW III.5)."""
+    rng = np.random.default_rng(k)
+    xn = 2.0
+    hist = xn - np.concatenate([[0.0], np.cumsum(rng.uniform(0.3, 1.2, k))])  # x_n, x_{n-1}, ...
+    h = rng.uniform(0.2, 1.5)
+    psi_prev = [xn - hist[i + 1] for i in range(k - 1)]
+    psi, beta, g = oracle.abm_coefficients(k, h, psi_prev)
+    for deg in range(k + 1):
+        coef = rng.standard_normal(deg + 1)
+        f = np.polynomial.Polynomial(coef)
+        F = f.integ()
+        dd = _divided(hist[:k], f(hist[:k]))
+        phi = [np.prod(psi_prev[:j]) * dd[j] for j in range(k)]
+        star = [beta[j] * phi[j] for j in range(k)]
+        pred = h * sum(g[j] * star[j] for j in range(k))
+        exact = F(xn + h) - F(xn)
+        if deg < k:
+            assert pred == pytest.approx(exact, rel=1e-11, abs=1e-11)
+        phik = f(xn + h) - sum(star)
+        corr = pred + h * g[k] * phik
+        assert corr == pytest.approx(exact, rel=1e-10, abs=1e-10)
+
+
+def test_vcabm5_matches_scipy(oracle):
+    """VCABM5 at tight tolerance reproduces a tight scipy DOP853 solution of the same RHS."""
+    scipy_integrate = pytest.importorskip("scipy.integrate")
+    mf = gen_mesh("RectOkada", 8e3, 4e3, 1e3, 1e3, 90.0)
+    mu = 3e10
+    gf = oracle.gf_ff(mf, mu, mu, fourier=True)
+    N = mf.nx * mf.nξ
+    o = np.ones((mf.nx, mf.nξ))
+    vpl = 1e-9
+    p = RateStateQuasiDynamicProperty(0.015 * o, 0.019 * o, 0.012 * o, 5e7 * o, mu / (2 * 3044.0), vpl, 0.6, vpl)
+    m = oracle.OracleModel(gf, p)
+    th0 = 0.012 / vpl * (1 + 0.01 * np.linspace(-1, 1, N))
+    u0 = np.concatenate([np.full(N, vpl), th0, np.zeros(N)])
+    T = 3.15e7
+    u1, st = m.integrate(u0, 0.0, T, reltol=1e-10, abstol=1e-14, dt0=1e-3, alg="VCABM5")
+    assert st.status == 0 and st.t == T
+    assert st.nrhs == 2 * st.naccept + st.nreject + 1  # PECE: two evaluations per accepted step
+    ref = scipy_integrate.solve_ivp(lambda t, y: m.ode(y), (0.0, T), u0, method="DOP853", rtol=1e-12, atol=1e-16)
+    np.testing.assert_allclose(u1, ref.y[:, -1], rtol=1e-7)
