@@ -145,10 +145,15 @@ long long gbc_model_state_len(const gbc_model* m);
 
 /* ---- On-device adaptive integration (stands in for OrdinaryDiffEq's solve, src/io.jl:125-130) */
 
+#define GBC_ALG_TSIT5 0   /* Tsitouras 5(4), PI step control (the reference's tests) */
+#define GBC_ALG_VCABM5 1  /* variable-coefficient Adams-Bashforth-Moulton, PECE, orders 1-5 (the
+                             reference's example, examples/otf-with-mantle.jl:160-162) */
+
 typedef struct gbc_solver_opts {
     double reltol, abstol;   /* error norm: RMS of err / (abstol + reltol * max(|u|, |u_new|)) */
     double dt0, dtmax, dtmin;
     long long maxiters;
+    int alg;                 /* GBC_ALG_*; 0 = Tsit5. Ensembles and the serving batch use Tsit5. */
 } gbc_solver_opts;
 
 typedef struct gbc_solver_stats {

@@ -713,7 +713,7 @@ static int integrate_common(gbc_model* m, double* u_dev, double t0, double t1, c
         if (int rc = theta_transform(u_dev + m->N, m->N, 1, m->stream)) return rc;
     }
     int rc = integrator_run(m->integ, args, u_dev, t0, t1, o->reltol, o->abstol, o->dt0, o->dtmax,
-                            o->dtmin, o->maxiters, m->stream, rec);
+                            o->dtmin, o->maxiters, m->stream, rec, o->alg);
     if (args.log_theta) {
         if (int rc2 = theta_transform(u_dev + m->N, m->N, 0, m->stream)) return rc2;
     }

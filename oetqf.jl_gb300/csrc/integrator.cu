@@ -1,5 +1,7 @@
-// Device-resident Tsit5 (Tsitouras 2011, 5(4) pair) with a PI step-size controller, standing in
-// for the reference's OrdinaryDiffEq caller (src/io.jl:125-130, test/tests.jl:11).
+// Device-resident adaptive integrators standing in for the reference's OrdinaryDiffEq caller
+// (src/io.jl:125-130): Tsit5 (Tsitouras 2011, 5(4) pair) with a PI step-size controller, as in the
+// reference's tests (test/tests.jl:11), and VCABM5 (variable-coefficient Adams-Bashforth-Moulton
+// in PECE mode, orders 1..5), as in the reference's example (examples/otf-with-mantle.jl:160-162).
 //
 // One step = 6 x (stage combination + RHS) + error norm/controller + commit, all on the device:
 // the controller kernel reads the error norm, accepts or rejects, and writes the next dt into
@@ -147,6 +149,204 @@ __global__ void k_clear_accept(Ctrl* c) {
     c->record = 0;
 }
 
+// ---- VCABM5 ---------------------------------------------------------------------------------------
+// Krogh's modified divided differences (Hairer, Norsett & Wanner, Solving ODEs I, sec. III.5;
+// Shampine & Gordon 1975). With x_{n+1} = x_n + h: psi_i = x_{n+1} - x_{n-i} = h + psi_{i-1}(prev),
+// beta_0 = 1, beta_i = beta_{i-1} psi_{i-1} / psi_{i-1}(prev), g_j = c_j(1) from c_0(q) = 1/q,
+// c_j(q) = c_{j-1}(q) - c_{j-1}(q+1) h / psi_{j-1}. Predict y^p = y + h sum_{j<k} g_j beta_j Phi_j,
+// evaluate f^p, correct y_{n+1} = y^p + h g_k (f^p - sum_{j<k} beta_j Phi_j), error
+// h (g_k - g_{k-1}) (f^p - sum beta_j Phi_j); an accepted step evaluates f_{n+1} and updates
+// Phi_0 = f_{n+1}, Phi_{j+1} = Phi_j(new) - beta_j Phi_j(old). The order rises by one per accepted
+// step up to 5 and restarts at 1 after three rejections in a row.
+constexpr int kAbmMax = 5;
+
+__global__ void k_abm_coef(Ctrl* c) {
+    if (c->done) return;
+    const int k = c->k;
+    const double h = c->dt;
+    c->kq = k;
+    c->psi[0] = h;
+    for (int i = 1; i < k; ++i) c->psi[i] = h + c->psi_prev[i - 1];
+    c->beta[0] = 1.0;
+    for (int i = 1; i < k; ++i) c->beta[i] = c->beta[i - 1] * c->psi[i - 1] / c->psi_prev[i - 1];
+    double cq[kAbmMax + 3] = {0};
+    for (int q = 1; q <= k + 1; ++q) cq[q] = 1.0 / q;
+    c->g[0] = cq[1];
+    for (int j = 1; j <= k; ++j) {
+        const double r = h / c->psi[j - 1];
+        for (int q = 1; q <= k + 1 - j; ++q) cq[q] = cq[q] - cq[q + 1] * r;
+        c->g[j] = cq[1];
+    }
+}
+
+struct PhiPtrs {
+    double* p[kAbmMax + 1];
+};
+
+// y^p = u + h sum_{j<k} g_j beta_j Phi_j and sv = sum_{j<k} beta_j Phi_j
+__global__ void k_abm_predict(long long n, const double* __restrict__ u, PhiPtrs P, double* __restrict__ yp,
+                              double* __restrict__ sv, const Ctrl* __restrict__ c) {
+    if (c->done) return;
+    const int k = c->kq;
+    const double h = c->dt;
+    double beta[kAbmMax], g[kAbmMax];
+#pragma unroll
+    for (int j = 0; j < kAbmMax; ++j) {
+        beta[j] = c->beta[j];
+        g[j] = c->g[j];
+    }
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double sacc = 0.0, acc = 0.0;
+#pragma unroll
+        for (int j = 0; j < kAbmMax; ++j) {
+            if (j < k) {
+                const double pj = beta[j] * P.p[j][i];
+                sacc += pj;
+                acc = fma(g[j], pj, acc);
+            }
+        }
+        sv[i] = sacc;
+        yp[i] = u[i] + h * acc;
+    }
+}
+
+// corrector, error norm partials; the last block to finish runs the step controller
+__global__ void k_abm_correct_control(long long n, const double* __restrict__ u, const double* __restrict__ yp,
+                                      const double* __restrict__ fp, const double* __restrict__ sv,
+                                      double* __restrict__ un, double* __restrict__ partial, Ctrl* c) {
+    if (c->done) return;
+    __shared__ double red[32];
+    __shared__ int last;
+    const int k = c->kq;
+    const double h = c->dt, rtol = c->reltol, atol = c->abstol;
+    const double gk = c->g[k], ce = h * (c->g[k] - c->g[k - 1]);
+    double ss = 0.0;
+    int bad = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double pk = fp[i] - sv[i];
+        const double yn = yp[i] + h * gk * pk;
+        un[i] = yn;
+        // with ψ = ln θ an absolute ψ error equals a relative θ error: scale it by reltol
+        const double sc = (c->log_theta && i >= c->th_lo && i < c->th_hi) ? atol + rtol
+                                                                             : atol + rtol * fmax(fabs(u[i]), fabs(yn));
+        const double r = ce * pk / sc;
+        ss = fma(r, r, ss);
+        bad |= !isfinite(yn);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = bad ? INFINITY : ss;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += red[w];
+        partial[blockIdx.x] = b;
+        __threadfence();
+        const unsigned prev = atomicAdd(&c->blocks_done, 1u);
+        last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    double tot = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) tot += ((volatile double*)partial)[b];
+    c->blocks_done = 0;
+    double EEst = sqrt(tot / (double)n);
+    if (!isfinite(EEst)) EEst = INFINITY;
+    const double qmin = 0.2, qmax = 2.0, gam = 0.8;
+    const double fac = gam * pow(EEst, -1.0 / (k + 1));
+    c->iters += 1;
+    c->nrhs += 1;
+    double dtn;
+    if (EEst <= 1.0) {
+        const double tn = c->t + h;
+        c->t = (tn >= c->t1) ? c->t1 : tn;
+        c->accept = 1;
+        c->skip2 = 0;
+        c->nrhs += 1;
+        c->naccept += 1;
+        c->record = (c->stride > 0 && c->naccept % c->stride == 0) ? 1 : 0;
+        for (int i = 0; i < k; ++i) c->psi_prev[i] = c->psi[i];
+        if (c->k < kAbmMax) c->k += 1;
+        c->fails = 0;
+        dtn = h * fmin(qmax, fmax(qmin, fac));
+    } else {
+        c->accept = 0;
+        c->skip2 = 1;
+        c->nreject += 1;
+        if (++c->fails >= 3) c->k = 1;
+        dtn = h * fmax(qmin, fmin(gam, isfinite(fac) ? fac : qmin));
+    }
+    if (c->t >= c->t1) {
+        c->done = 1;
+        c->status = 0;
+    } else if (dtn < c->dtmin || !isfinite(dtn) || c->iters >= c->maxiters) {
+        c->done = 1;
+        c->status = -5;
+    }
+    if (dtn > c->dtmax) dtn = c->dtmax;
+    const double rem = c->t1 - c->t;
+    if (dtn >= rem) dtn = rem;
+    c->dt = dtn;
+}
+
+// accepted step: u <- y_{n+1}, Phi update with f_{n+1} (fn) and this step's beta, ring record
+__global__ void k_abm_commit(long long n, double* __restrict__ u, const double* __restrict__ un,
+                             const double* __restrict__ fn, PhiPtrs P, const Ctrl* __restrict__ c) {
+    if (!c->accept) return;
+    const int k = c->kq;
+    double beta[kAbmMax];
+#pragma unroll
+    for (int j = 0; j < kAbmMax; ++j) beta[j] = c->beta[j];
+    const bool rec = c->record && c->ring_cap > 0;
+    double* ur = rec ? c->u_ring + (c->nrec % c->ring_cap) * n : nullptr;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double v = un[i];
+        u[i] = v;
+        double nw = fn[i];
+#pragma unroll
+        for (int j = 0; j < kAbmMax; ++j) {
+            if (j < k) {
+                const double old = P.p[j][i];
+                P.p[j][i] = nw;
+                nw = nw - beta[j] * old;
+            }
+        }
+        P.p[k][i] = nw;
+        if (rec) ur[i] = (c->log_theta && i >= c->th_lo && i < c->th_hi) ? exp(v) : v;
+    }
+    if (rec && blockIdx.x == 0 && threadIdx.x == 0) c->t_ring[c->nrec % c->ring_cap] = c->t;
+}
+
+static int enqueue_abm_step(Integrator& I, const RhsArgs& rhs0, double* u, cudaStream_t s) {
+    const long long n = I.n;
+    const int g = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 4);
+    PhiPtrs P;
+    for (int j = 0; j <= kAbmMax; ++j) P.p[j] = I.phi[j];
+    double* yp = I.y;
+    double* fp = I.k[1];
+    double* sv = I.k[2];
+    double* fn = I.k[3];
+    k_abm_coef<<<1, 1, 0, s>>>(I.ctrl);
+    GBC_CUDA(cudaGetLastError());
+    k_abm_predict<<<g, 256, 0, s>>>(n, u, P, yp, sv, I.ctrl);
+    GBC_CUDA(cudaGetLastError());
+    RhsArgs rhs = rhs0;
+    rhs.skip = &I.ctrl->done;
+    if (int rc = launch_rhs(rhs, yp, fp, s)) return rc;
+    k_abm_correct_control<<<I.err_blocks, 256, 0, s>>>(n, u, yp, fp, sv, I.un, I.partial, I.ctrl);
+    GBC_CUDA(cudaGetLastError());
+    rhs.skip = &I.ctrl->skip2;  // the corrected point is evaluated only for accepted steps
+    if (int rc = launch_rhs(rhs, I.un, fn, s)) return rc;
+    k_abm_commit<<<g, 256, 0, s>>>(n, u, I.un, fn, P, I.ctrl);
+    GBC_CUDA(cudaGetLastError());
+    k_clear_accept<<<1, 1, 0, s>>>(I.ctrl);
+    GBC_CUDA(cudaGetLastError());
+    return 0;
+}
+
 int integrator_alloc(Integrator& I, long long n) {
     if (I.n == n && I.y) return 0;
     integrator_free(I);
@@ -172,6 +372,7 @@ void integrator_free(Integrator& I) {
     if (I.step_exec) cudaGraphExecDestroy(I.step_exec);
     if (I.t_ring) cudaFree(I.t_ring);
     if (I.u_ring) cudaFree(I.u_ring);
+    for (int j = 0; j <= kAbmMax; ++j) if (I.phi[j]) cudaFree(I.phi[j]);
     I = Integrator();
 }
 
@@ -199,8 +400,16 @@ static int enqueue_step(Integrator& I, const RhsArgs& rhs0, double* u, cudaStrea
 
 int integrator_run(Integrator& I, const RhsArgs& rhs0, double* u, double t0, double t1, double reltol,
                    double abstol, double dt0, double dtmax, double dtmin, long long maxiters,
-                   cudaStream_t s, Recorder* rec) {
+                   cudaStream_t s, Recorder* rec, int alg) {
+    if (alg != 0 && alg != 1) return fail(GBC_EINVAL, "unknown integrator (GBC_ALG_TSIT5 or GBC_ALG_VCABM5)");
+    if (alg == 1 && !I.phi[0])
+        for (int j = 0; j <= kAbmMax; ++j) {
+            GBC_CUDA(cudaMalloc(&I.phi[j], sizeof(double) * I.n));
+            GBC_CUDA(cudaMemsetAsync(I.phi[j], 0, sizeof(double) * I.n, s));
+        }
     Ctrl h{};
+    h.alg = alg;
+    h.k = 1;
     if (rec && rec->stride > 0) {
         const long long cap = 32;  // >= the steps of one graph launch
         if (I.ring_cap != cap) {
@@ -234,9 +443,10 @@ int integrator_run(Integrator& I, const RhsArgs& rhs0, double* u, double t0, dou
     GBC_CUDA(cudaMemcpyAsync(I.ctrl, I.ctrl_host, sizeof(Ctrl), cudaMemcpyHostToDevice, s));
     RhsArgs rhs = rhs0;
     rhs.skip = nullptr;
-    if (int rc = launch_rhs(rhs, u, I.k[0], s)) return rc;  // FSAL seed k0 = f(u0)
+    // FSAL seed k0 = f(u0) (Tsit5) or Phi_0 = f(u0) (VCABM5)
+    if (int rc = launch_rhs(rhs, u, alg == 1 ? I.phi[0] : I.k[0], s)) return rc;
     // capture a group of steps once per (model, state pointer); relaunch until done
-    const int group = 8;
+    const int group = (alg == 1) ? 16 : 8;
     if (I.step_exec) {
         cudaGraphExecDestroy(I.step_exec);
         I.step_exec = nullptr;
@@ -244,7 +454,7 @@ int integrator_run(Integrator& I, const RhsArgs& rhs0, double* u, double t0, dou
     cudaGraph_t graph;
     GBC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     int rc = 0;
-    for (int k = 0; k < group && rc == 0; ++k) rc = enqueue_step(I, rhs0, u, s);
+    for (int k = 0; k < group && rc == 0; ++k) rc = (alg == 1) ? enqueue_abm_step(I, rhs0, u, s) : enqueue_step(I, rhs0, u, s);
     cudaError_t ce = cudaStreamEndCapture(s, &graph);
     if (rc) return rc;
     GBC_CUDA(ce);

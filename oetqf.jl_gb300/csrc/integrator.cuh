@@ -14,6 +14,11 @@ struct Ctrl {
     int done, status, accept, log_theta;
     unsigned int blocks_done;
     long long th_lo, th_hi;  // θ slot of the state; holds ψ = ln θ when log_theta
+    // VCABM5 (alg 1): current order k, order of the step in flight kq, consecutive rejections,
+    // psi of the last accepted step, this step's psi / beta / Adams weights g, and skip2 = no
+    // evaluation at the corrected point (rejected or finished)
+    int alg, k, kq, fails, skip2;
+    double psi_prev[5], psi[6], beta[6], g[7];
     // recording (wsolve-style): every stride-th accepted step into a device ring of ring_cap slots
     int stride, record;
     long long nrec, ring_cap;
@@ -44,13 +49,15 @@ struct Integrator {
     double* t_ring = nullptr;      // device ring of the recorder (ring_cap slots)
     double* u_ring = nullptr;
     long long ring_cap = 0;
+    double* phi[6] = {};  // VCABM: modified divided differences Phi_0..Phi_5 (allocated on first use)
 };
 
 int integrator_alloc(Integrator& I, long long n);
 void integrator_free(Integrator& I);
-// Integrates u (device) from t0 to t1. Fills the host mirror of Ctrl.
+// Integrates u (device) from t0 to t1 with Tsit5 (alg 0) or VCABM5 (alg 1). Fills the host mirror
+// of Ctrl.
 int integrator_run(Integrator& I, const RhsArgs& rhs, double* u, double t0, double t1,
                    double reltol, double abstol, double dt0, double dtmax, double dtmin,
-                   long long maxiters, cudaStream_t s, Recorder* rec = nullptr);
+                   long long maxiters, cudaStream_t s, Recorder* rec = nullptr, int alg = 0);
 
 }  // namespace gbc

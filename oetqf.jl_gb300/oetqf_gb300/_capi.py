@@ -36,7 +36,11 @@ class HexMesh(ctypes.Structure):
 
 
 class SolverOpts(ctypes.Structure):
-    _fields_ = [("reltol", D), ("abstol", D), ("dt0", D), ("dtmax", D), ("dtmin", D), ("maxiters", LL)]
+    _fields_ = [("reltol", D), ("abstol", D), ("dt0", D), ("dtmax", D), ("dtmin", D), ("maxiters", LL), ("alg", I)]
+
+
+GBC_ALG_TSIT5, GBC_ALG_VCABM5 = 0, 1
+ALGS = {"Tsit5": GBC_ALG_TSIT5, "VCABM5": GBC_ALG_VCABM5}
 
 
 class SolverStats(ctypes.Structure):

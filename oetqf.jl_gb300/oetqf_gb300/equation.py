@@ -183,10 +183,10 @@ class GB300Model:
         C.check(C.lib().gbc_rhs_dev(self.h, float(t), ctypes.c_void_p(u_ptr), ctypes.c_void_p(du_ptr)))
 
     def integrate(self, u: np.ndarray, t0: float, t1: float, reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=np.inf,
-                  dtmin=1e-14, maxiters=10**9):
-        """On-device Tsit5 from t0 to t1; returns (u(t1), stats)."""
+                  dtmin=1e-14, maxiters=10**9, alg="Tsit5"):
+        """On-device Tsit5 or VCABM5 from t0 to t1; returns (u(t1), stats)."""
         u = np.ascontiguousarray(u, dtype=np.float64).copy()
-        o = C.SolverOpts(reltol, abstol, dt, dtmax if np.isfinite(dtmax) else 1e300, dtmin, maxiters)
+        o = C.SolverOpts(reltol, abstol, dt, dtmax if np.isfinite(dtmax) else 1e300, dtmin, maxiters, C.ALGS[alg])
         s = C.SolverStats()
         rc = C.lib().gbc_integrate(self.h, C.ptr(u), float(t0), float(t1), ctypes.byref(o), ctypes.byref(s))
         if rc < 0 and rc != -5:
@@ -194,8 +194,8 @@ class GB300Model:
         return u, s
 
     def integrate_dev(self, u_ptr: int, t0: float, t1: float, reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=np.inf,
-                      dtmin=1e-14, maxiters=10**9):
-        o = C.SolverOpts(reltol, abstol, dt, dtmax if np.isfinite(dtmax) else 1e300, dtmin, maxiters)
+                      dtmin=1e-14, maxiters=10**9, alg="Tsit5"):
+        o = C.SolverOpts(reltol, abstol, dt, dtmax if np.isfinite(dtmax) else 1e300, dtmin, maxiters, C.ALGS[alg])
         s = C.SolverStats()
         rc = C.lib().gbc_integrate_dev(self.h, ctypes.c_void_p(u_ptr), float(t0), float(t1), ctypes.byref(o),
                                        ctypes.byref(s))
@@ -251,8 +251,9 @@ def assemble(*args, **kwargs) -> ODEProblem:
     raise TypeError("assemble: expected (gf, p, u0, tspan) or (gf11, gf12, gf21, gf22, pf, pa, u0, tspan)")
 
 
-def solve(prob: ODEProblem, reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=np.inf, maxiters=10**9):
-    """Integrates the problem on the device (Tsit5) and returns (u(t_end) as ArrayPartition, stats)."""
+def solve(prob: ODEProblem, alg="Tsit5", reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=np.inf, maxiters=10**9):
+    """solve(prob, alg; ...) (src/io.jl:125-130): integrates on the device with "Tsit5" or "VCABM5" (the
+    reference's example solver) and returns (u(t_end) as ArrayPartition, stats)."""
     u, st = prob.p.integrate(prob.u0.flat(), prob.tspan[0], prob.tspan[1], reltol=reltol, abstol=abstol, dt=dt,
-                             dtmax=dtmax, maxiters=maxiters)
+                             dtmax=dtmax, maxiters=maxiters, alg=alg)
     return ArrayPartition.like(prob.u0, u), st

@@ -17,10 +17,10 @@ from .equation import ArrayPartition, ODEProblem
 
 
 def integrate_record(model, u0: np.ndarray, t0: float, t1: float, stride: int = 1, max_records: int = 10000,
-                     reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=np.inf, dtmin=1e-14, maxiters=10**9):
+                     reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=np.inf, dtmin=1e-14, maxiters=10**9, alg="Tsit5"):
     """gbc_integrate_record: returns (u(t1), stats, t_records, u_records)."""
     u = np.ascontiguousarray(u0, dtype=np.float64).copy()
-    o = C.SolverOpts(reltol, abstol, dt, dtmax if np.isfinite(dtmax) else 1e300, dtmin, maxiters)
+    o = C.SolverOpts(reltol, abstol, dt, dtmax if np.isfinite(dtmax) else 1e300, dtmin, maxiters, C.ALGS[alg])
     s = C.SolverStats()
     t_out = np.zeros(max_records)
     u_out = np.zeros(max_records * u.size)
