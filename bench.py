@@ -35,10 +35,14 @@ from oetqf_gb300.workloads import (YEAR, fault_ensemble, large_fault_with_mantle
                                    strike_slip_fault, strike_slip_with_mantle)
 
 SOLVER = dict(reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=0.2 * YEAR)
-# Tsit5 steps (accepted + rejected) this controller takes over each workload's horizon, as measured
-# by the device integrator (the CPU oracle's controller is the same and takes the same steps over
-# the horizons the parity tests cover); used to turn a bounded CPU sample into sim-yr/s.
-STEPS_FOR_HORIZON = {"fault-mantle-1000x2500-f64": 42388, "fault-800-f64": 4757}
+# Right-hand-side evaluations each integrator takes over a workload's horizon, as counted by the
+# device integrator (the oracle restates the same methods and controllers and takes the same steps
+# over the horizons the parity tests cover: 28543 and 12381 for the 800-patch fault, counted by
+# both); used to turn a bounded CPU sample into sim-yr/s.
+RHS_FOR_HORIZON = {("fault-mantle-1000x2500-f64", "Tsit5"): 6 * 42388 + 1,
+                   ("fault-mantle-1000x2500-f64", "VCABM5"): 138665,
+                   ("fault-800-f64", "Tsit5"): 28543, ("fault-800-f64", "VCABM5"): 12381}
+WORKLOADS = ["fault-mantle-1000x2500-f64", "fault-800-f64"]
 # DRAM bytes (read + write) of one k_rows launch from ncu, per workload
 # (profiles/k_rows_fault-mantle-1000x2500-f64.md)
 NCU_TRAFFIC = {"fault-mantle-1000x2500-f64": 2044237000 + 2987264,
@@ -135,25 +139,27 @@ def cpu_oracle_model(cm, gfs=None):
     return O, O.OracleModel(gf11, cm.pf, g12, g21, g22, cm.pa), "stand-in mantle values (timing is value-independent)"
 
 
-def cpu_oracle_sample(cm, name, gfs=None, budget_s=20.0):
-    """Times the oracle's Tsit5 (all host threads) over a bounded number of steps of the full-size
-    workload and scales by the controller's step count for the whole horizon."""
+def cpu_oracle_sample(cm, name, alg, gfs=None, budget_s=20.0, nrhs_horizon=None):
+    """Times the oracle (all host threads) over a bounded number of steps of the full-size workload
+    with the same integrator and scales by the RHS evaluations that integrator takes for the whole
+    horizon (from the table, or as counted on the device in the same run)."""
     O, om, how = cpu_oracle_model(cm, gfs)
     t0 = time.perf_counter()
     om.ode(cm.u0)
     t_rhs = time.perf_counter() - t0
-    steps = int(min(500, max(3, budget_s / (6.0 * max(t_rhs, 1e-6)))))
+    per_step = 6.0 if alg == "Tsit5" else 2.0
+    steps = int(min(1500, max(3, budget_s / (per_step * max(t_rhs, 1e-6)))))
     t0 = time.perf_counter()
     _, st = om.integrate(cm.u0, 0.0, cm.horizon, reltol=SOLVER["reltol"], abstol=SOLVER["abstol"], dt0=SOLVER["dt"],
-                         maxiters=steps)
+                         maxiters=steps, alg=alg)
     wall = time.perf_counter() - t0
-    done = st.naccept + st.nreject
-    per_step = wall / max(done, 1)
-    total = per_step * STEPS_FOR_HORIZON[name]
+    per_rhs = wall / max(st.nrhs, 1)
+    total_rhs = RHS_FOR_HORIZON.get((name, alg), nrhs_horizon)
+    total = per_rhs * total_rhs
     return {"value": (cm.horizon / YEAR) / total, "unit": "sim-yr/s", "cores": O.num_threads(), "kind": "port",
-            "sample": f"{done} Tsit5 steps of the full-size workload on the C/OpenMP FP64 oracle "
-                      f"({per_step * 1e3:.2f} ms/step, Green's functions: {how}), scaled to the "
-                      f"{STEPS_FOR_HORIZON[name]} steps the same controller takes for {cm.horizon / YEAR:.0f} yr"}
+            "sample": f"{st.naccept + st.nreject} {alg} steps ({st.nrhs} RHS) of the full-size workload on the "
+                      f"C/OpenMP FP64 oracle ({per_rhs * 1e3:.2f} ms/RHS, Green's functions: {how}), scaled to the "
+                      f"{total_rhs} RHS evaluations the same integrator takes for {cm.horizon / YEAR:.0f} yr"}
 
 
 def run_reference(args):
@@ -163,7 +169,7 @@ def run_reference(args):
     cm = workload(args.workload)
     vals = []
     for _ in range(args.steps):
-        vals.append(cpu_oracle_sample(cm, args.workload, budget_s=args.cpu_budget / max(args.steps, 1)))
+        vals.append(cpu_oracle_sample(cm, args.workload, args.alg, budget_s=args.cpu_budget / max(args.steps, 1)))
     v = statistics.median([x["value"] for x in vals])
     base = vals[0]
     base["value"] = v
@@ -171,7 +177,7 @@ def run_reference(args):
             "ms_per_step": (cm.horizon / YEAR) / v / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded splitmix64)", "impl": "reference",
             "config": {"workload": args.workload, "fault_patches": cm.N, "mantle_cells": cm.ne,
-                       "horizon_yr": cm.horizon / YEAR},
+                       "horizon_yr": cm.horizon / YEAR, "solver": f"{args.alg} reltol 1e-6 abstol 1e-8 dt0 1e-8 s dtmax 0.2 yr"},
             "cpu_baseline": base, "e2e": {"value": v, "unit": "sim-yr/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -212,7 +218,7 @@ def run_gpu(args):
     for _ in range(args.warmup):
         u.copy_(torch.tensor(cm.u0, device="cuda"))
         torch.cuda.synchronize()
-        m.integrate_dev(u.data_ptr(), 0.0, 0.01 * YEAR, **SOLVER)
+        m.integrate_dev(u.data_ptr(), 0.0, 0.01 * YEAR, alg=args.alg, **SOLVER)
     u.copy_(torch.tensor(cm.u0, device="cuda"))
     torch.cuda.synchronize()
     K = args.steps
@@ -225,13 +231,14 @@ def run_gpu(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = C.kernel_launches()
     e0.record(stream)
-    naccept = nreject = 0
+    naccept = nreject = nrhs = 0
     for k in range(K):
-        st = m.integrate_dev(u.data_ptr(), float(edges[k]), float(edges[k + 1]), **SOLVER)
+        st = m.integrate_dev(u.data_ptr(), float(edges[k]), float(edges[k + 1]), alg=args.alg, **SOLVER)
         if st.status != 0:
             raise SystemExit(f"integration failed in window {k}: status {st.status}")
         naccept += st.naccept
         nreject += st.nreject
+        nrhs += st.nrhs
     e1.record(stream)
     e1.synchronize()
     torch.cuda.synchronize()
@@ -293,8 +300,8 @@ def run_gpu(args):
         ref.assemble_gf(cm.mf, cm.ma, cm.lam, cm.mu)
         ref.set_fault_props(cm.pf)
         ref.set_mantle_props(cm.pa)
-        ua, _ = ref.integrate(cm.u0, 0.0, YEAR, **SOLVER)
-        ub, _ = m.integrate(cm.u0, 0.0, YEAR, **SOLVER)
+        ua, _ = ref.integrate(cm.u0, 0.0, YEAR, alg=args.alg, **SOLVER)
+        ub, _ = m.integrate(cm.u0, 0.0, YEAR, alg=args.alg, **SOLVER)
         err_vs_f64 = float(np.abs(ub[:cm.N] - ua[:cm.N]).max() / np.abs(ua[:cm.N]).max())
         del ref
     # e2e: the same horizon through the host-buffer C-ABI call (pinned host state, H2D + D2H per window)
@@ -304,7 +311,7 @@ def run_gpu(args):
     x0, x1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     x0.record(stream)
     for k in range(K):
-        out, st = m.integrate(un, float(edges[k]), float(edges[k + 1]), **SOLVER)
+        out, st = m.integrate(un, float(edges[k]), float(edges[k + 1]), alg=args.alg, **SOLVER)
         un[:] = out
     x1.record(stream)
     x1.synchronize()
@@ -318,7 +325,9 @@ def run_gpu(args):
             "config": {"workload": args.workload, "fault_patches": cm.N, "mantle_cells": cm.ne, "horizon_yr": sim_yr,
                        "precision": "f64" if args.storage == "f64" else
                        "mantle + fault rows as FP32 pairs (hi + lo), compensated FP32 dot products, FP64 results and friction",
-                       "solver": "Tsit5 reltol 1e-6 abstol 1e-8 dt0 1e-8 s dtmax 0.2 yr",
+                       "solver": f"{args.alg} reltol 1e-6 abstol 1e-8 dt0 1e-8 s dtmax 0.2 yr (the reference example's "
+                                 "settings, examples/otf-with-mantle.jl:160-162)",
+                       "rhs_evals": nrhs,
                        "l2": "inputs larger than L2 (Green's functions read every RHS)", "parallelism": "replicas",
                        "rk_steps": naccept + nreject, "rk_rejected": nreject, "assembly_s": round(t_asm, 3)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -335,7 +344,8 @@ def run_gpu(args):
         line["max_slip_rate_rel_err_vs_f64_1yr"] = err_vs_f64
     if not args.no_cpu:
         gfs = tuple(m.export_gf(w) for w in (C.GBC_GF12, C.GBC_GF21, C.GBC_GF22)) if cm.ne else None
-        line["cpu_baseline"] = cpu_oracle_sample(cm, args.workload, gfs=gfs, budget_s=args.cpu_budget)
+        line["cpu_baseline"] = cpu_oracle_sample(cm, args.workload, args.alg, gfs=gfs, budget_s=args.cpu_budget,
+                                                 nrhs_horizon=nrhs)
     print(json.dumps(line), flush=True)
 
 
@@ -389,7 +399,7 @@ def run_mixed_large(args):
         e0.record(stream)
         steps = 0
         for k in range(args.steps):
-            st = m.integrate_dev(u.data_ptr(), float(edges[k]), float(edges[k + 1]), **SOLVER)
+            st = m.integrate_dev(u.data_ptr(), float(edges[k]), float(edges[k + 1]), alg=args.alg, **SOLVER)
             steps += st.naccept + st.nreject
         e1.record(stream)
         e1.synchronize()
@@ -403,7 +413,7 @@ def run_mixed_large(args):
     ach = mx["bytes"] / (mx["rhs_ms"] / 1e3) / 1e9
     line = _base_line(years / (mx["ms"] / 1e3), args, 1,
                       {"workload": f"fault-mantle-4096x8000-{args.precision}", "fault_patches": N, "mantle_cells": cm.ne,
-                       "window_yr": years, "assembly_s": round(t_asm, 2), "rk_steps": mx["steps"],
+                       "window_yr": years, "assembly_s": round(t_asm, 2), "rk_steps": mx["steps"], "solver": args.alg,
                        "storage": f"{args.precision} with FP32 scale per 128x128 block, FP32 accumulate; FP32 Toeplitz (shared memory); FP64 friction, ln-theta state, error norm",
                        "l2": "inputs larger than L2"}, mx["ms"] / args.steps, args.precision)
     line["roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
@@ -539,9 +549,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbcycle", choices=["gbcycle", "reference"])
     ap.add_argument("--workload", default="fault-mantle-1000x2500-f64",
-                    choices=list(STEPS_FOR_HORIZON) + ["fault-mantle-4096x8000-mixed", "ensemble-256", "serving",
+                    choices=WORKLOADS + ["fault-mantle-4096x8000-mixed", "ensemble-256", "serving",
                                                        "ensemble-profile"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "f16"])
+    ap.add_argument("--alg", default="VCABM5", choices=["VCABM5", "Tsit5"],
+                    help="integrator of the single-model workloads (VCABM5: the reference example's solver)")
     ap.add_argument("--fp64-sample", type=int, default=8)
     ap.add_argument("--requests", type=int, default=32)
     ap.add_argument("--hbm-budget-gb", type=float, default=64.0)

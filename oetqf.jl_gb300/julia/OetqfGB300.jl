@@ -85,6 +85,43 @@ function gpu_ode(du::ArrayPartition, u::ArrayPartition, m::GB300Model, t)
     return nothing
 end
 
+struct GbcSolverOpts
+    reltol::Cdouble; abstol::Cdouble; dt0::Cdouble; dtmax::Cdouble; dtmin::Cdouble
+    maxiters::Clonglong
+    alg::Cint
+end
+
+mutable struct GbcSolverStats
+    naccept::Clonglong; nreject::Clonglong; nrhs::Clonglong
+    t::Cdouble; dt::Cdouble
+    status::Cint
+end
+
+"""
+    solve_gb300(prob, alg; reltol, abstol, dt, dtmax, maxiters)
+
+`solve(prob, alg; ...)` (src/io.jl:125-130) with the whole integration on the device: `VCABM5()` or
+`Tsit5()` with the same options; returns (u(t_end) as an ArrayPartition like `prob.u0`, stats).
+"""
+function solve_gb300(prob::ODEProblem, alg; reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=Inf, dtmin=1e-14,
+                     maxiters::Integer=10^9)
+    m = prob.p::GB300Model
+    code = alg isa VCABM5 ? Cint(1) : alg isa Tsit5 ? Cint(0) : throw(ArgumentError("VCABM5() or Tsit5()"))
+    o = GbcSolverOpts(reltol, abstol, dt, isfinite(dtmax) ? dtmax : 1e300, dtmin, maxiters, code)
+    st = GbcSolverStats(0, 0, 0, 0.0, 0.0, 0)
+    u = reduce(vcat, (vec(copy(x)) for x in prob.u0.x))
+    rc = ccall((:gbc_integrate, libgbc), Cint,
+               (Ptr{Cvoid}, Ptr{Cdouble}, Cdouble, Cdouble, Ref{GbcSolverOpts}, Ref{GbcSolverStats}),
+               m.h, u, prob.tspan[1], prob.tspan[2], o, st)
+    rc == 0 || rc == -5 || check(rc)
+    out = deepcopy(prob.u0)
+    off = 0
+    for x in out.x
+        copyto!(x, 1, u, off + 1, length(x)); off += length(x)
+    end
+    return out, st
+end
+
 "assemble(gf, p, u0, tspan) with the RHS on the GB300 (src/BEM/equation.jl:81-89)."
 function assemble_gb300(gf::AbstractArray, p::RateStateQuasiDynamicProperty, u0::ArrayPartition, tspan::NTuple{2})
     nx, nξ = size(u0.x[1])
