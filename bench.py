@@ -444,15 +444,16 @@ def run_ensemble(args):
     u0 = np.zeros(e.state_len)
     for i, mm in enumerate(models):
         u0[e.offsets[i]:e.offsets[i] + mm.u0.size] = mm.u0
-    best, tim = e.autotune(u0, steps=200, **SOLVER)
+    alg = args.alg
+    best, tim = e.autotune(u0, steps=200, alg=alg, **SOLVER)
     stream = torch.cuda.ExternalStream(e.stream)
     for _ in range(args.warmup):
-        e.integrate(u0, 0.0, 0.01 * YEAR, **SOLVER)
+        e.integrate(u0, 0.0, 0.01 * YEAR, alg=alg, **SOLVER)
     u = torch.tensor(u0, device="cuda")
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    st = e.integrate_dev(u.data_ptr(), 0.0, years * YEAR, **SOLVER)
+    st = e.integrate_dev(u.data_ptr(), 0.0, years * YEAR, alg=alg, **SOLVER)
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
@@ -460,7 +461,7 @@ def run_ensemble(args):
     value = 256 * years / (ms / 1e3)
     # e2e through the host-buffer call
     t0 = time.perf_counter()
-    e.integrate(u0, 0.0, years * YEAR, **SOLVER)
+    e.integrate(u0, 0.0, years * YEAR, alg=alg, **SOLVER)
     e2e_s = time.perf_counter() - t0
     # plain FP64 GPU path on a sample of members
     idx = np.linspace(0, 255, args.fp64_sample).astype(int)
@@ -471,7 +472,7 @@ def run_ensemble(args):
         g.assemble_gf(mm.mf, None, mm.lam, mm.mu)
         g.set_fault_props(mm.pf)
         t0 = time.perf_counter()
-        g.integrate(mm.u0, 0.0, years * YEAR, **SOLVER)
+        g.integrate(mm.u0, 0.0, years * YEAR, alg=alg, **SOLVER)
         tot += time.perf_counter() - t0
     fp64_total = tot / len(idx) * 256
     # error vs the FP64 oracle over 2 years on a few members
@@ -484,20 +485,20 @@ def run_ensemble(args):
         es = Ensemble([(mm.mf.nx, mm.mf.nξ)])
         es.assemble(0, mm.mf, mm.lam, mm.mu)
         es.set_fault_props(0, mm.pf)
-        ug, _ = es.integrate(mm.u0, 0.0, 2.0 * YEAR, **SOLVER)
+        ug, _ = es.integrate(mm.u0, 0.0, 2.0 * YEAR, alg=alg, **SOLVER)
         gf = O.gf_ff(mm.mf, mm.lam, mm.mu, fourier=True)
-        uc, _ = O.OracleModel(gf, mm.pf).integrate(mm.u0, 0.0, 2.0 * YEAR, reltol=SOLVER["reltol"], abstol=SOLVER["abstol"], dt0=SOLVER["dt"], dtmax=SOLVER["dtmax"])
+        uc, _ = O.OracleModel(gf, mm.pf).integrate(mm.u0, 0.0, 2.0 * YEAR, reltol=SOLVER["reltol"], abstol=SOLVER["abstol"], dt0=SOLVER["dt"], dtmax=SOLVER["dtmax"], alg=alg)
         N = mm.N
         errs.append(float(np.abs(ug[:N] - uc[:N]).max() / np.abs(uc[:N]).max()))
     line = _base_line(value, args, 1, {"workload": "ensemble-256-fault-only", "models": 256, "patches_total": int(sum(mm.N for mm in models)),
                                        "patch_range": [int(min(mm.N for mm in models)), int(max(mm.N for mm in models))],
-                                       "horizon_yr": years, "cta_threads": best, "autotune_s": tim,
+                                       "horizon_yr": years, "solver": alg, "cta_threads": best, "autotune_s": tim,
                                        "rk_steps_min_mean_max": [int(steps.min()), float(steps.mean()), int(steps.max())],
                                        "slowest_member_patches": int(models[int(np.argmax(steps))].N),
                                        "precision": "FP32 rFFT convolution in shared memory; FP64 friction, ln-theta state, stages, error norm (PI gain factors in FP32)",
                                        "regroup": "models still running move to 2/4/8-CTA clusters as others finish",
                                        "l2": "state and spectra L2-resident (per-model working set)"}, ms, "f32+f64")
-    line["fp64_gpu"] = {"value": 256 * years / fp64_total, "sample": f"{len(idx)} members integrated one at a time with the FP64 single-model path, scaled to 256"}
+    line["fp64_gpu"] = {"value": 256 * years / fp64_total, "sample": f"{len(idx)} members integrated one at a time with the FP64 single-model path ({alg}), scaled to 256"}
     line["speedup_vs_fp64_gpu"] = value / line["fp64_gpu"]["value"]
     line["max_slip_rate_rel_err_vs_fp64_oracle_2yr"] = max(errs)
     line["e2e"] = {"value": 256 * years / e2e_s, "unit": "sim-yr/s", "h2d_bytes_per_step": int(u0.nbytes), "d2h_bytes_per_step": int(u0.nbytes)}

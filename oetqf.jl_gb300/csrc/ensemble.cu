@@ -246,9 +246,33 @@ struct EnsCtl {
     double t, dt, t1, qold;
     long long naccept, nreject, iters, maxiters;
     int done, status, go, stop;
+    // VCABM5: order, order of the step in flight, consecutive rejections, psi of the last accepted
+    // step, and this step's psi, beta and Adams weights (the oracle's orc_abm_coefficients)
+    int k, kq, fails;
+    double psi_prev[5], psi[6], beta[6], g[7];
 };
 
-template <int BS>
+__device__ __forceinline__ void ens_abm_coef(EnsCtl& c, double h) {
+    const int k = c.k;
+    c.kq = k;
+    c.psi[0] = h;
+    for (int i = 1; i < k; ++i) c.psi[i] = h + c.psi_prev[i - 1];
+    c.beta[0] = 1.0;
+    for (int i = 1; i < k; ++i) c.beta[i] = c.beta[i - 1] * c.psi[i - 1] / c.psi_prev[i - 1];
+    double cq[8] = {0};
+    for (int q = 1; q <= k + 1; ++q) cq[q] = 1.0 / q;
+    c.g[0] = cq[1];
+    for (int j = 1; j <= k; ++j) {
+        const double r = h / c.psi[j - 1];
+        for (int q = 1; q <= k + 1 - j; ++q) cq[q] = cq[q] - cq[q + 1] * r;
+        c.g[j] = cq[1];
+    }
+}
+
+// ALG 0: Tsit5 (6 RHS per step); ALG 1: VCABM5 (PECE: 1 RHS per step + 1 per accepted step;
+// the modified divided differences Phi_0..Phi_5 live in the stage buffers k[0..5], k[6] holds f at
+// the predicted and then at the corrected point)
+template <int BS, int ALG>
 __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
     extern __shared__ __align__(16) float sm[];
     __shared__ double red[BS / 32];
@@ -288,6 +312,10 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
         c.t = m.t; c.dt = m.dt; c.t1 = m.t1; c.qold = m.qold;
         c.naccept = m.naccept; c.nreject = m.nreject; c.iters = m.iters; c.maxiters = m.maxiters;
         c.done = m.done; c.status = m.status; c.go = 0; c.stop = 0;
+        c.k = m.abm_k > 0 ? m.abm_k : 1;
+        c.kq = c.k;
+        c.fails = m.abm_fails;
+        for (int i = 0; i < 5; ++i) c.psi_prev[i] = m.psi_prev[i];
         xfail = 0;
         if (clus) {
             for (int b = 0; b < 4; ++b) mbar_init(&S.mb[b], 1);
@@ -333,77 +361,147 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
     for (int step = 0; step < A.budget && !xfail; ++step) {
         if (c.stop) break;  // decided by the last step's controller, identically in every rank
         const double dt = c.dt;
-        for (int s = 1; s < 7; ++s) {
-            double* dst = (s == 6) ? un : y;
-            float* xb = S.xr + (size_t)(rx & 1) * N;
-            // the three components' FMA chains interleaved (FP64 latency, not throughput, binds here);
-            // cluster ranks publish v - vpl of their slice to every peer as they go
-            for (int i = lo + threadIdx.x; i < hi; i += BS) {
-                double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
-                for (int r = 0; r < s; ++r) {
-                    const double a = e_ta[s][r];
-                    acc0 = fma(a, kk[r][i], acc0);
-                    acc1 = fma(a, kk[r][N + i], acc1);
-                    acc2 = fma(a, kk[r][2 * N + i], acc2);
-                }
-                const double vnew = u[i] + dt * acc0;
-                dst[i] = vnew;
-                dst[N + i] = u[N + i] + dt * acc1;
-                dst[2 * N + i] = u[2 * N + i] + dt * acc2;
-                if (clus) {
-                    const float x = (float)(vnew - m.vpl);
-                    xb[i] = x;
-                    for (int d = 1; d < csize; ++d) push_f32(xb + i, x, &S.mb[rx & 1], (rank + d) % csize);
-                }
-            }
-            if (clus) {
-                collect(rx & 1, xbytes);
-                if (xfail) break;
-            }
-            ens_rhs<BS>(m, A, S, dst, kk[s], lo, hi, clus ? xb : nullptr);
-            ++rx;
-        }
-        if (xfail) break;
-        // error norm: per 32-patch chunk, lane i sums r^2 over the three components, then a fixed
-        // shuffle tree; the chunk sums (pushed to every rank) are added in chunk order, identically
-        // in every rank, together with rank 0's wall-clock stop flag
         const int e = step & 1;
         double* prb = S.pr + (size_t)e * (nch + 1);
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        for (int ch = c0 + warp; ch < c1; ch += BS / 32) {
-            const int i = 32 * ch + lane;
-            double ss = 0.0;
-            int bad = 0;
-            if (i < N) {
-                double ev[3], r[3];
-#pragma unroll
-                for (int comp = 0; comp < 3; ++comp) ev[comp] = 0.0;
-#pragma unroll
-                for (int s = 0; s < 7; ++s)
-#pragma unroll
-                    for (int comp = 0; comp < 3; ++comp) ev[comp] = fma(e_te[s], kk[s][comp * N + i], ev[comp]);
-#pragma unroll
-                for (int comp = 0; comp < 3; ++comp) {
-                    const int g = comp * N + i;
-                    const double unv = un[g];
-                    // ψ = ln θ: an absolute ψ error is a relative θ error, scaled by reltol
-                    const double sc = (comp == 1 && m.log_theta) ? A.abstol + A.reltol
-                                                                 : A.abstol + A.reltol * fmax(fabs(u[g]), fabs(unv));
-                    r[comp] = (ev[comp] * dt) / sc;
-                    bad |= !isfinite(unv);
+        if (ALG == 0) {
+            for (int s = 1; s < 7; ++s) {
+                double* dst = (s == 6) ? un : y;
+                float* xb = S.xr + (size_t)(rx & 1) * N;
+                // the three components' FMA chains interleaved (FP64 latency, not throughput, binds here);
+                // cluster ranks publish v - vpl of their slice to every peer as they go
+                for (int i = lo + threadIdx.x; i < hi; i += BS) {
+                    double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
+                    for (int r = 0; r < s; ++r) {
+                        const double a = e_ta[s][r];
+                        acc0 = fma(a, kk[r][i], acc0);
+                        acc1 = fma(a, kk[r][N + i], acc1);
+                        acc2 = fma(a, kk[r][2 * N + i], acc2);
+                    }
+                    const double vnew = u[i] + dt * acc0;
+                    dst[i] = vnew;
+                    dst[N + i] = u[N + i] + dt * acc1;
+                    dst[2 * N + i] = u[2 * N + i] + dt * acc2;
+                    if (clus) {
+                        const float x = (float)(vnew - m.vpl);
+                        xb[i] = x;
+                        for (int d = 1; d < csize; ++d) push_f32(xb + i, x, &S.mb[rx & 1], (rank + d) % csize);
+                    }
                 }
-                ss = fma(r[0], r[0], ss);  // components summed in order 0, 1, 2
-                ss = fma(r[1], r[1], ss);
-                ss = fma(r[2], r[2], ss);
+                if (clus) {
+                    collect(rx & 1, xbytes);
+                    if (xfail) break;
+                }
+                ens_rhs<BS>(m, A, S, dst, kk[s], lo, hi, clus ? xb : nullptr);
+                ++rx;
             }
-            for (int o = 16; o > 0; o >>= 1) {
-                ss += __shfl_xor_sync(0xffffffffu, ss, o);
-                bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+            if (xfail) break;
+            // error norm: per 32-patch chunk, lane i sums r^2 over the three components, then a fixed
+            // shuffle tree; the chunk sums (pushed to every rank) are added in chunk order, identically
+            // in every rank, together with rank 0's wall-clock stop flag
+            for (int ch = c0 + warp; ch < c1; ch += BS / 32) {
+                const int i = 32 * ch + lane;
+                double ss = 0.0;
+                int bad = 0;
+                if (i < N) {
+                    double ev[3], r[3];
+    #pragma unroll
+                    for (int comp = 0; comp < 3; ++comp) ev[comp] = 0.0;
+    #pragma unroll
+                    for (int s = 0; s < 7; ++s)
+    #pragma unroll
+                        for (int comp = 0; comp < 3; ++comp) ev[comp] = fma(e_te[s], kk[s][comp * N + i], ev[comp]);
+    #pragma unroll
+                    for (int comp = 0; comp < 3; ++comp) {
+                        const int g = comp * N + i;
+                        const double unv = un[g];
+                        // ψ = ln θ: an absolute ψ error is a relative θ error, scaled by reltol
+                        const double sc = (comp == 1 && m.log_theta) ? A.abstol + A.reltol
+                                                                     : A.abstol + A.reltol * fmax(fabs(u[g]), fabs(unv));
+                        r[comp] = (ev[comp] * dt) / sc;
+                        bad |= !isfinite(unv);
+                    }
+                    ss = fma(r[0], r[0], ss);  // components summed in order 0, 1, 2
+                    ss = fma(r[1], r[1], ss);
+                    ss = fma(r[2], r[2], ss);
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    ss += __shfl_xor_sync(0xffffffffu, ss, o);
+                    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+                }
+                if (lane == 0) {
+                    const double val = bad ? INFINITY : ss;
+                    prb[ch] = val;
+                    for (int d = 1; d < csize; ++d) push_f64(prb + ch, val, &S.mb[2 + e], (rank + d) % csize);
+                }
             }
-            if (lane == 0) {
-                const double val = bad ? INFINITY : ss;
-                prb[ch] = val;
-                for (int d = 1; d < csize; ++d) push_f64(prb + ch, val, &S.mb[2 + e], (rank + d) % csize);
+        } else {
+            // VCABM5 step: coefficients, predictor (publishing v), f at the predicted point, corrector
+            // with the error chunks; f at the corrected point and the Phi update after acceptance
+            // every thread is done with the last step's beta (its Phi update) before thread 0 rewrites it
+            __syncthreads();
+            if (threadIdx.x == 0) ens_abm_coef(c, dt);
+            __syncthreads();
+            const int kq = c.kq;
+            {
+                float* xb = S.xr + (size_t)(rx & 1) * N;
+                for (int i = lo + threadIdx.x; i < hi; i += BS) {
+                    double acc[3] = {0.0, 0.0, 0.0};
+                    for (int j = 0; j < kq; ++j) {
+                        const double bj = c.beta[j], gj = c.g[j];
+#pragma unroll
+                        for (int comp = 0; comp < 3; ++comp) acc[comp] = fma(gj, bj * kk[j][comp * N + i], acc[comp]);
+                    }
+                    const double vnew = u[i] + dt * acc[0];
+                    y[i] = vnew;
+                    y[N + i] = u[N + i] + dt * acc[1];
+                    y[2 * N + i] = u[2 * N + i] + dt * acc[2];
+                    if (clus) {
+                        const float x = (float)(vnew - m.vpl);
+                        xb[i] = x;
+                        for (int d = 1; d < csize; ++d) push_f32(xb + i, x, &S.mb[rx & 1], (rank + d) % csize);
+                    }
+                }
+                if (clus) {
+                    collect(rx & 1, xbytes);
+                    if (xfail) break;
+                }
+                ens_rhs<BS>(m, A, S, y, kk[6], lo, hi, clus ? xb : nullptr);
+                ++rx;
+            }
+            const double gk = c.g[kq], ce = dt * (c.g[kq] - c.g[kq - 1]);
+            for (int ch = c0 + warp; ch < c1; ch += BS / 32) {
+                const int i = 32 * ch + lane;
+                double ss = 0.0;
+                int bad = 0;
+                if (i < N) {
+                    double r[3];
+#pragma unroll
+                    for (int comp = 0; comp < 3; ++comp) {
+                        const int g = comp * N + i;
+                        double sacc = 0.0;
+                        for (int j = 0; j < kq; ++j) sacc += c.beta[j] * kk[j][g];
+                        const double pk = kk[6][g] - sacc;
+                        const double yn = y[g] + dt * gk * pk;
+                        un[g] = yn;
+                        const double sc = (comp == 1 && m.log_theta) ? A.abstol + A.reltol
+                                                                     : A.abstol + A.reltol * fmax(fabs(u[g]), fabs(yn));
+                        r[comp] = (ce * pk) / sc;
+                        bad |= !isfinite(yn);
+                    }
+                    ss = fma(r[0], r[0], ss);
+                    ss = fma(r[1], r[1], ss);
+                    ss = fma(r[2], r[2], ss);
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    ss += __shfl_xor_sync(0xffffffffu, ss, o);
+                    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+                }
+                if (lane == 0) {
+                    const double val = bad ? INFINITY : ss;
+                    prb[ch] = val;
+                    for (int d = 1; d < csize; ++d) push_f64(prb + ch, val, &S.mb[2 + e], (rank + d) % csize);
+                }
             }
         }
         if (writer) {
@@ -423,7 +521,48 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
             for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
             red[0] = tot;  // lane 0 below
         }
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == 0 && ALG == 1) {
+            const double tot = red[0];
+            double EEst = sqrt(tot / (double)(3 * N));
+            if (!isfinite(EEst)) EEst = INFINITY;
+            const int kq = c.kq;
+            // step factor 0.8 EEst^(-1/(k+1)) within [0.2, 2] (at most 0.8 after a rejection), in FP32
+            // like the PI gains; acceptance compares the FP64 norm
+            const double fac = 0.8 * (double)exp2f(-log2f((float)EEst) / (float)(kq + 1));
+            c.iters += 1;
+            double dtn;
+            int acc = 0;
+            if (EEst <= 1.0) {
+                const double tn = c.t + dt;
+                c.t = (tn >= c.t1) ? c.t1 : tn;
+                c.naccept += 1;
+                acc = 1;
+                for (int i = 0; i < kq; ++i) c.psi_prev[i] = c.psi[i];
+                if (c.k < 5) c.k += 1;
+                c.fails = 0;
+                dtn = dt * fmin(2.0, fmax(0.2, fac));
+            } else {
+                c.nreject += 1;
+                if (++c.fails >= 3) c.k = 1;
+                dtn = dt * fmax(0.2, fmin(0.8, isfinite(fac) ? fac : 0.2));
+            }
+            if (c.t >= c.t1) { c.done = 1; c.status = 0; }
+            else if (dtn < A.dtmin || !isfinite(dtn) || c.iters >= c.maxiters) { c.done = 1; c.status = -5; }
+            if (dtn > A.dtmax) dtn = A.dtmax;
+            const double rem = c.t1 - c.t;
+            if (dtn >= rem) dtn = rem;
+            c.dt = dtn;
+            c.go = acc;
+            c.stop = c.done || (prb[nch] != 0.0);
+            if (rank == 0) {
+                M.t = c.t; M.dt = c.dt; M.qold = c.qold;
+                M.naccept = c.naccept; M.nreject = c.nreject; M.iters = c.iters;
+                M.done = c.done; M.status = c.status;
+                M.abm_k = c.k; M.abm_fails = c.fails;
+                for (int i = 0; i < 5; ++i) M.psi_prev[i] = c.psi_prev[i];
+            }
+        }
+        if (threadIdx.x == 0 && ALG == 0) {
             const double tot = red[0];
             double EEst = sqrt(tot / (double)(3 * N));
             if (!isfinite(EEst)) EEst = INFINITY;
@@ -464,12 +603,39 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
             }
         }
         __syncthreads();
-        if (c.go) {
+        if (c.go && ALG == 0) {
             for (int comp = 0; comp < 3; ++comp)
                 for (int i = lo + threadIdx.x; i < hi; i += BS) {
                     const int g = comp * N + i;
                     u[g] = un[g];
                     kk[0][g] = kk[6][g];
+                }
+        } else if (c.go) {
+            // f at the corrected point, then Phi_0 = f_{n+1}, Phi_{j+1} = Phi_j(new) - beta_j Phi_j(old)
+            float* xb = S.xr + (size_t)(rx & 1) * N;
+            if (clus) {
+                for (int i = lo + threadIdx.x; i < hi; i += BS) {
+                    const float x = (float)(un[i] - m.vpl);
+                    xb[i] = x;
+                    for (int d = 1; d < csize; ++d) push_f32(xb + i, x, &S.mb[rx & 1], (rank + d) % csize);
+                }
+                collect(rx & 1, xbytes);
+                if (xfail) break;
+            }
+            ens_rhs<BS>(m, A, S, un, kk[6], lo, hi, clus ? xb : nullptr);
+            ++rx;
+            const int kq = c.kq;
+            for (int comp = 0; comp < 3; ++comp)
+                for (int i = lo + threadIdx.x; i < hi; i += BS) {
+                    const int g = comp * N + i;
+                    double nw = kk[6][g];
+                    for (int j = 0; j < kq; ++j) {
+                        const double old = kk[j][g];
+                        kk[j][g] = nw;
+                        nw = nw - c.beta[j] * old;
+                    }
+                    kk[kq][g] = nw;
+                    u[g] = un[g];
                 }
         }
     }
@@ -540,7 +706,8 @@ void ens_groups(const EnsModel* models, int n, int maxc, int boost, std::vector<
 
 template <int BS>
 static int launch_cluster(const EnsArgs& A, int nmod, int csize, size_t smem, cudaStream_t s) {
-    if (int rc = set_smem_limit((const void*)k_ensemble<BS>, (int)smem)) return rc;
+    void (*kern)(EnsArgs) = (A.alg == 1) ? k_ensemble<BS, 1> : k_ensemble<BS, 0>;
+    if (int rc = set_smem_limit((const void*)kern, (int)smem)) return rc;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(nmod * csize));
     cfg.blockDim = dim3(BS);
@@ -553,13 +720,14 @@ static int launch_cluster(const EnsArgs& A, int nmod, int csize, size_t smem, cu
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    GBC_CUDA(cudaLaunchKernelEx(&cfg, k_ensemble<BS>, A));
+    GBC_CUDA(cudaLaunchKernelEx(&cfg, kern, A));
     return 0;
 }
 
 int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtmax, double dtmin,
-                   unsigned long long budget_ns, int block, size_t smem, cudaStream_t main) {
+                   unsigned long long budget_ns, int block, size_t smem, cudaStream_t main, int alg) {
     EnsArgs A{};
+    A.alg = alg;
     A.models = L.models; A.nmodels = L.n; A.order = L.order; A.ctl = L.ctl;
     A.reltol = reltol; A.abstol = abstol; A.dtmax = dtmax; A.dtmin = dtmin;
     A.budget = 1 << 20;
@@ -911,6 +1079,7 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
     if (!e || !u_dev || !t0 || !t1 || !o) return fail(GBC_EINVAL, "null argument");
     if (!(o->reltol > 0) || !(o->abstol >= 0) || !(o->dt0 > 0) || !(o->dtmax > 0) || o->maxiters <= 0)
         return fail(GBC_EINVAL, "invalid solver options");
+    if (o->alg != GBC_ALG_TSIT5 && o->alg != GBC_ALG_VCABM5) return fail(GBC_EINVAL, "unknown integrator");
     for (int i = 0; i < e->n; ++i)
         if (!e->has_gf[i] || !e->has_props[i]) return fail(GBC_ESTATE, "ensemble model " + std::to_string(i) + " is missing its Green's function or properties");
     for (int i = 0; i < e->n; ++i) {
@@ -924,6 +1093,9 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
         m.status = 0;
         m.done = (t1[i] <= t0[i]) ? 1 : 0;
         m.started = 0;
+        m.abm_k = 1;
+        m.abm_fails = 0;
+        for (int j = 0; j < 5; ++j) m.psi_prev[j] = 0.0;
         m.log_theta = e->log_theta && !m.done;
         m.logged = m.log_theta;
     }
@@ -946,7 +1118,8 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
         GBC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         int rc = 0;
         for (int k = 0; k < 2 && !rc; ++k)
-            rc = ens_run_groups(e->lp, o->reltol, o->abstol, o->dtmax, o->dtmin, 100000000ull, e->block, e->smem, s);
+            rc = ens_run_groups(e->lp, o->reltol, o->abstol, o->dtmax, o->dtmin, 100000000ull, e->block, e->smem, s,
+                                o->alg);
         cudaError_t ce = cudaStreamEndCapture(s, &g);
         if (rc) return rc;
         GBC_CUDA(ce);
@@ -984,7 +1157,8 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
     for (int i = 0; i < e->n; ++i) {
         const EnsModel& m = e->host[i];
         if (stats) {
-            stats[i].naccept = m.naccept; stats[i].nreject = m.nreject; stats[i].nrhs = 6 * m.iters + 1;
+            stats[i].naccept = m.naccept; stats[i].nreject = m.nreject;
+            stats[i].nrhs = (o->alg == GBC_ALG_VCABM5) ? m.iters + m.naccept + 1 : 6 * m.iters + 1;
             stats[i].t = m.t; stats[i].dt = m.dt; stats[i].status = m.status;
         }
         if (m.status != 0) status = GBC_ESOLVER;

@@ -24,6 +24,8 @@ struct EnsModel {
     double t, dt, t1, qold;
     long long naccept, nreject, iters, maxiters;
     int status, done, started, logged;  // logged: θ slot holds ln θ during this integration
+    int abm_k, abm_fails;                // VCABM5: order (0 = start at 1) and consecutive rejections
+    double psi_prev[5];                  // VCABM5: psi of the last accepted step
 };
 
 struct EnsArgs {
@@ -31,7 +33,8 @@ struct EnsArgs {
     int nmodels;
     const int* order;            // models of this launch, grouped by cluster size: order[first + i]
     int first;
-    int* ctl;                    // per model: stop flag of the current step (written by rank 0)
+    int* ctl;
+    int alg;                     // 0: Tsit5, 1: VCABM5                    // per model: stop flag of the current step (written by rank 0)
     double reltol, abstol, dtmax, dtmin;
     int budget;                      // step cap per launch and model
     unsigned long long budget_ns;    // wall-clock budget per launch (all models stay busy until done)
@@ -65,7 +68,7 @@ int ens_launch_prepare(EnsLaunch& L, EnsModel* d_models, const EnsModel* host, i
                        cudaStream_t s);
 // one persistent launch per group: each model runs until done or budget_ns of wall clock
 int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtmax, double dtmin,
-                   unsigned long long budget_ns, int block, size_t smem, cudaStream_t main);
+                   unsigned long long budget_ns, int block, size_t smem, cudaStream_t main, int alg = 0);
 // θ <-> ln θ on the state of every descriptor with `logged` set
 int ens_theta(EnsModel* d_models, int n, int to_log, cudaStream_t s);
 void count_launches(long long n);

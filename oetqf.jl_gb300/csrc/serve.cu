@@ -237,7 +237,7 @@ static void finish_fault(gbc_server* s, Req& r) {
     r.dmem = nullptr;
     r.stats.naccept = m.naccept;
     r.stats.nreject = m.nreject;
-    r.stats.nrhs = 6 * m.iters + 1;
+    r.stats.nrhs = (s->batch_opts.alg == GBC_ALG_VCABM5) ? m.iters + m.naccept + 1 : 6 * m.iters + 1;
     r.stats.t = m.t;
     r.stats.dt = m.dt;
     r.stats.status = m.status;
@@ -418,7 +418,7 @@ static void scheduler(gbc_server* s) {
         if (!rc && cudaMemcpyAsync(s->d_desc, h.data(), sizeof(EnsModel) * n, cudaMemcpyHostToDevice, s->batch) != cudaSuccess) rc = GBC_ECUDA;
         if (!rc) rc = ens_launch_prepare(s->lp, s->d_desc, h.data(), n, 8, ens_boost(n), s->batch);
         if (!rc) rc = ens_run_groups(s->lp, s->batch_opts.reltol, s->batch_opts.abstol, s->batch_opts.dtmax,
-                                     s->batch_opts.dtmin, s->slice_ns, s->block, smem, s->batch);
+                                     s->batch_opts.dtmin, s->slice_ns, s->block, smem, s->batch, s->batch_opts.alg);
         if (!rc && cudaMemcpyAsync(h.data(), s->d_desc, sizeof(EnsModel) * n, cudaMemcpyDeviceToHost, s->batch) != cudaSuccess) rc = GBC_ECUDA;
         if (!rc && cudaStreamSynchronize(s->batch) != cudaSuccess) rc = GBC_ECUDA;
         std::vector<std::shared_ptr<Req>> fin;

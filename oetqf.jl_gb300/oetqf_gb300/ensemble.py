@@ -77,33 +77,35 @@ class Ensemble:
     def set_log_theta(self, on: bool):
         C.check(C.lib().gbc_ensemble_set_log_theta(self.h, int(bool(on))))
 
-    def _opts(self, reltol, abstol, dt, dtmax, maxiters):
-        return C.SolverOpts(reltol, abstol, dt, dtmax if np.isfinite(dtmax) else 1e300, 1e-14, maxiters)
+    def _opts(self, reltol, abstol, dt, dtmax, maxiters, alg="Tsit5"):
+        return C.SolverOpts(reltol, abstol, dt, dtmax if np.isfinite(dtmax) else 1e300, 1e-14, maxiters, C.ALGS[alg])
 
-    def integrate(self, u, t0, t1, reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=np.inf, maxiters=10**9):
-        """Host state (concatenated (v, θ, δ) per model) from t0[i] to t1[i]; returns (u, stats)."""
+    def integrate(self, u, t0, t1, reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=np.inf, maxiters=10**9, alg="Tsit5"):
+        """Host state (concatenated (v, θ, δ) per model) from t0[i] to t1[i] with "Tsit5" or "VCABM5";
+        returns (u, stats)."""
         u = np.ascontiguousarray(u, dtype=np.float64).copy()
         t0 = np.ascontiguousarray(np.broadcast_to(t0, (self.n,)), dtype=np.float64)
         t1 = np.ascontiguousarray(np.broadcast_to(t1, (self.n,)), dtype=np.float64)
         st = (C.SolverStats * self.n)()
-        o = self._opts(reltol, abstol, dt, dtmax, maxiters)
+        o = self._opts(reltol, abstol, dt, dtmax, maxiters, alg)
         rc = C.lib().gbc_ensemble_integrate(self.h, C.ptr(u), C.ptr(t0), C.ptr(t1), ctypes.byref(o), st)
         if rc < 0 and rc != -5:
             C.check(rc)
         return u, list(st)
 
-    def integrate_dev(self, u_ptr, t0, t1, reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=np.inf, maxiters=10**9):
+    def integrate_dev(self, u_ptr, t0, t1, reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=np.inf, maxiters=10**9,
+                      alg="Tsit5"):
         t0 = np.ascontiguousarray(np.broadcast_to(t0, (self.n,)), dtype=np.float64)
         t1 = np.ascontiguousarray(np.broadcast_to(t1, (self.n,)), dtype=np.float64)
         st = (C.SolverStats * self.n)()
-        o = self._opts(reltol, abstol, dt, dtmax, maxiters)
+        o = self._opts(reltol, abstol, dt, dtmax, maxiters, alg)
         rc = C.lib().gbc_ensemble_integrate_dev(self.h, ctypes.c_void_p(u_ptr), C.ptr(t0), C.ptr(t1), ctypes.byref(o), st)
         if rc < 0 and rc != -5:
             C.check(rc)
         return list(st)
 
     def autotune(self, u0, steps=200, candidates=(128, 256, 512), **solver):
-        """Times the same fixed number of Tsit5 steps for every model (a horizon too long to reach,
+        """Times the same fixed number of steps for every model (a horizon too long to reach,
         capped by maxiters) with each CTA size and keeps the fastest: per-step cost, not the mix of
         cheap and expensive steps in a short time window, decides."""
         solver = {k: v for k, v in solver.items() if k != "maxiters"}

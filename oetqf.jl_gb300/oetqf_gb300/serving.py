@@ -57,9 +57,10 @@ def _sigs():
 
 
 class Server:
-    def __init__(self, hbm_budget_gb=64.0, reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=1e300, maxiters=10**9):
+    def __init__(self, hbm_budget_gb=64.0, reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=1e300, maxiters=10**9,
+                 alg="Tsit5"):
         L = _sigs()
-        self.opts = C.SolverOpts(reltol, abstol, dt, dtmax, 1e-14, maxiters)
+        self.opts = C.SolverOpts(reltol, abstol, dt, dtmax, 1e-14, maxiters, C.ALGS[alg])
         h = ctypes.c_void_p()
         C.check(L.gbc_server_create(hbm_budget_gb * 2**30, ctypes.byref(self.opts), ctypes.byref(h)))
         self.h = h

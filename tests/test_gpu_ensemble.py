@@ -96,3 +96,33 @@ def test_regrouping_keeps_trajectories():
     assert [s.t for s in sb] == list(t1)
     assert [s.naccept for s in sa] == [s.naccept for s in sb]
     np.testing.assert_array_equal(ua, ub)
+
+
+def test_vcabm5_ensemble(oracle):
+    """VCABM5 inside the persistent launch: each member matches the oracle's VCABM5 (same method,
+    FP32 convolution) and the state is bitwise independent of block size, cluster size and
+    regrouping, as for Tsit5."""
+    models = fault_ensemble(n_models=12, n_range=(100, 1300), seed=37)
+    e, u0 = _build(models)
+    T = 2 * YEAR
+    t1 = np.linspace(0.3, 1.0, len(models)) * T
+    u, st = e.integrate(u0, 0.0, t1, reltol=1e-8, abstol=1e-10, dt=1e-3, alg="VCABM5")
+    assert all(s.status == 0 for s in st) and [s.t for s in st] == list(t1)
+    assert all(s.nrhs == s.naccept + s.naccept + s.nreject + 1 for s in st)
+    for i in (0, 5, 11):
+        m = models[i]
+        gf = oracle.gf_ff(m.mf, m.lam, m.mu, fourier=True)
+        uc, sc = oracle.OracleModel(gf, m.pf).integrate(m.u0, 0.0, t1[i], reltol=1e-8, abstol=1e-10, dt0=1e-3,
+                                                         alg="VCABM5")
+        N = m.N
+        ui = u[e.offsets[i]:e.offsets[i] + 3 * N]
+        assert np.abs(ui[:N] - uc[:N]).max() / np.abs(uc[:N]).max() < 1e-4
+    outs = []
+    for block, maxc, rg in ((128, 1, False), (512, 8, True), (256, 2, True)):
+        e.set_block(block)
+        e.set_max_cluster(maxc)
+        e.set_regroup(rg)
+        outs.append(e.integrate(u0, 0.0, t1, reltol=1e-8, abstol=1e-10, dt=1e-3, alg="VCABM5")[0])
+    np.testing.assert_array_equal(outs[0], u)
+    np.testing.assert_array_equal(outs[1], u)
+    np.testing.assert_array_equal(outs[2], u)
