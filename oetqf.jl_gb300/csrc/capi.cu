@@ -414,7 +414,10 @@ int gbc_stress_gf_mm(const gbc_hex_mesh* ma, double lambda, double mu, const dou
     DevBuf rm, cm;
     if (int rc = rm.alloc((size_t)(R * R))) return rc;
     if (int rc = cm.alloc((size_t)(R * R))) return rc;
-    if (int rc = launch_gf_mm(h, lambda, mu, qc, qw, nq > 0 ? nq : 1, rm.p, (size_t)R, 0)) return rc;
+    MMGrid grid;
+    const bool structured = mm_grid(ma, grid);
+    if (int rc = launch_gf_mm(h, lambda, mu, qc, qw, nq > 0 ? nq : 1, rm.p, (size_t)R, 0, structured ? &grid : nullptr))
+        return rc;
     if (int rc = rm_to_cm(rm.p, (size_t)R, R, R, cm.p, 0)) return rc;
     g_launches += 2;
     GBC_CUDA(cudaMemcpy(out, cm.p, sizeof(double) * R * R, cudaMemcpyDeviceToHost));
@@ -619,7 +622,11 @@ int gbc_model_assemble(gbc_model* m, const gbc_fault_mesh* mf, const gbc_hex_mes
         if (int rc = quad_dev(qcoords, qweights, nq, keep, qc, qw, s)) return rc;
         if (int rc = launch_gf_fm(f, h, lambda, mu, ftype, nrept, buffer_ratio, qc, qw, nq > 0 ? nq : 1, m->gm.p, m->ldm, s)) return rc;
         if (int rc = launch_gf_mf(h, f, lambda, mu, ftype, m->g21.p, m->ld21, s)) return rc;
-        if (int rc = launch_gf_mm(h, lambda, mu, qc, qw, nq > 0 ? nq : 1, m->gm.p + m->npad, m->ldm, s)) return rc;
+        MMGrid grid;
+        const bool structured = mm_grid(ma, grid);
+        if (int rc = launch_gf_mm(h, lambda, mu, qc, qw, nq > 0 ? nq : 1, m->gm.p + m->npad, m->ldm, s,
+                                  structured ? &grid : nullptr))
+            return rc;
         g_launches += 3;
         m->has_g12 = m->has_g21 = m->has_g22 = true;
     }

@@ -4,6 +4,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "gbcycle.h"
 
@@ -54,8 +55,15 @@ int launch_gf_fm(const FaultDev& f, const HexDev& m, double lambda, double mu, i
 // mantle -> fault: rows i (fault patch), cols (p*ne + j), row-major with leading dim ld
 int launch_gf_mf(const HexDev& m, const FaultDev& f, double lambda, double mu, int ftype,
                  double* out, size_t ld, cudaStream_t s);
-// mantle-mantle: rows (k*ne + j), cols (p*ne + i), row-major with leading dim ld
+// structured mantle boxes: per-cell grid indices (see mm_grid)
+struct MMGrid {
+    int nX = 0, nY = 0, nZ = 0;
+    std::vector<int> ix, iy, iz, cell;
+};
+bool mm_grid(const gbc_hex_mesh* ma, MMGrid& g);
+// mantle-mantle: rows (k*ne + j), cols (p*ne + i), row-major with leading dim ld; with a grid, one
+// evaluation per distinct (offset, layers) key
 int launch_gf_mm(const HexDev& m, double lambda, double mu, const double* qc, const double* qw,
-                 int nq, double* out, size_t ld, cudaStream_t s);
+                 int nq, double* out, size_t ld, cudaStream_t s, const MMGrid* grid = nullptr);
 
 }  // namespace gbc

@@ -8,7 +8,10 @@
 // stack of Okada dislocation planes through the cuboid integrated over its thickness with
 // Gauss-Legendre panels: a uniform eigenstrain eps* equals a continuous stack of dislocations
 // with sym(b (x) n) = eps* per unit thickness.
+#include <algorithm>
+#include <cmath>
 #include <mutex>
+#include <vector>
 #include <set>
 #include <cuda_runtime.h>
 
@@ -303,6 +306,24 @@ __global__ void k_gf_mf(HexDev h, FaultDev f, double lam, double mu, int ftype,
     }
 }
 
+// stress components k at receiver cell jr (quadrature-averaged) from unit eigenstrain p in source
+// cell is (GF.jl:250-296)
+__device__ __forceinline__ void mm_pair(const HexDev& h, int jr, int is, double lam, double mu,
+                                        const double* __restrict__ qc, const double* __restrict__ qw, int nq,
+                                        double (&acc)[6][6]) {
+    for (int p = 0; p < 6; ++p)
+        for (int k = 0; k < 6; ++k) acc[p][k] = 0.0;
+    for (int q = 0; q < nq; ++q) {
+        const double rx = h.cx[jr] + qc[3 * q] * h.dx[jr] / 2.0;
+        const double ry = h.cy[jr] + qc[3 * q + 1] * h.dy[jr] / 2.0;
+        const double rz = h.cz[jr] + qc[3 * q + 2] * h.dz[jr] / 2.0;
+        double S[6][6];
+        hex8_unit_stresses(rx, ry, rz, h.qx[is], h.qy[is], h.qz[is], h.dx[is], h.dy[is], h.dz[is], lam, mu, S);
+        for (int p = 0; p < 6; ++p)
+            for (int k = 0; k < 6; ++k) acc[p][k] += S[p][k] * qw[q];
+    }
+}
+
 __global__ void k_gf_mm(HexDev h, double lam, double mu, const double* __restrict__ qc,
                         const double* __restrict__ qw, int nq, double* __restrict__ out, size_t ld) {
     const int ne = h.ne;
@@ -310,19 +331,41 @@ __global__ void k_gf_mm(HexDev h, double lam, double mu, const double* __restric
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
         const int is = (int)(t % ne), jr = (int)(t / ne);  // is: source cell, jr: receiver cell
-        double acc[6][6] = {};
-        for (int q = 0; q < nq; ++q) {
-            const double rx = h.cx[jr] + qc[3 * q] * h.dx[jr] / 2.0;
-            const double ry = h.cy[jr] + qc[3 * q + 1] * h.dy[jr] / 2.0;
-            const double rz = h.cz[jr] + qc[3 * q + 2] * h.dz[jr] / 2.0;
-            double S[6][6];
-            hex8_unit_stresses(rx, ry, rz, h.qx[is], h.qy[is], h.qz[is], h.dx[is], h.dy[is], h.dz[is],
-                               lam, mu, S);
-            for (int p = 0; p < 6; ++p)
-                for (int k = 0; k < 6; ++k) acc[p][k] += S[p][k] * qw[q];
-        }
+        double acc[6][6];
+        mm_pair(h, jr, is, lam, mu, qc, qw, nq, acc);
         for (int p = 0; p < 6; ++p)
             for (int k = 0; k < 6; ++k) out[((size_t)k * ne + jr) * ld + (size_t)p * ne + is] = acc[p][k];
+    }
+}
+
+// Structured boxes (a complete nX x nY x nZ grid of equal cells): an entry depends only on the
+// horizontal offset of the two cells and their layers (the half-space is invariant under horizontal
+// translation), so each key (dx, dy, layer_r, layer_s) is evaluated once on a representative pair
+// of the mesh and the dense matrix is filled from the table.
+__global__ void k_gf_mm_keys(HexDev h, double lam, double mu, const double* __restrict__ qc,
+                             const double* __restrict__ qw, int nq, const int2* __restrict__ reps, long long nkeys,
+                             double* __restrict__ table) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nkeys;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int2 r = reps[t];  // (receiver, source)
+        double acc[6][6];
+        mm_pair(h, r.x, r.y, lam, mu, qc, qw, nq, acc);
+        for (int p = 0; p < 6; ++p)
+            for (int k = 0; k < 6; ++k) table[t * 36 + p * 6 + k] = acc[p][k];
+    }
+}
+
+__global__ void k_gf_mm_expand(int ne, const int4* __restrict__ cell, int nX, int nY, int nZ,
+                               const double* __restrict__ table, double* __restrict__ out, size_t ld) {
+    const long long total = (long long)ne * ne;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int is = (int)(t % ne), jr = (int)(t / ne);
+        const int4 a = cell[jr], b = cell[is];  // (ix, iy, iz, -)
+        const long long key = (((long long)(a.x - b.x + nX - 1) * (2 * nY - 1) + (a.y - b.y + nY - 1)) * nZ + a.z) * nZ + b.z;
+        const double* v = table + key * 36;
+        for (int p = 0; p < 6; ++p)
+            for (int k = 0; k < 6; ++k) out[((size_t)k * ne + jr) * ld + (size_t)p * ne + is] = v[p * 6 + k];
     }
 }
 
@@ -376,12 +419,87 @@ int launch_gf_mf(const HexDev& m, const FaultDev& f, double lambda, double mu, i
     return 0;
 }
 
+// Host side: is the mesh a complete grid of equal cells (centres on uniform x and y grids with the
+// cell size as spacing, any set of depths, the same source-corner offsets)? Fills per-cell indices.
+bool mm_grid(const gbc_hex_mesh* ma, MMGrid& g) {
+    const int ne = ma->ne;
+    if (ne < 2) return false;
+    for (int i = 0; i < ne; ++i)
+        if (ma->dx[i] != ma->dx[0] || ma->dy[i] != ma->dy[0] || ma->dz[i] != ma->dz[0] ||
+            ma->qx[i] - ma->cx[i] != ma->qx[0] - ma->cx[0] || ma->qy[i] - ma->cy[i] != ma->qy[0] - ma->cy[0] ||
+            ma->qz[i] - ma->cz[i] != ma->qz[0] - ma->cz[0])
+            return false;
+    auto axis = [&](const double* c, double d, std::vector<int>& idx, int& n) {
+        double lo = c[0], hi = c[0];
+        for (int i = 1; i < ne; ++i) { lo = std::min(lo, c[i]); hi = std::max(hi, c[i]); }
+        n = (int)std::llround((hi - lo) / d) + 1;
+        idx.resize(ne);
+        for (int i = 0; i < ne; ++i) {
+            const double f = (c[i] - lo) / d;
+            const long long k = std::llround(f);
+            if (std::fabs(f - (double)k) > 1e-9) return false;
+            idx[i] = (int)k;
+        }
+        return n >= 1;
+    };
+    if (!axis(ma->cx, ma->dx[0], g.ix, g.nX) || !axis(ma->cy, ma->dy[0], g.iy, g.nY)) return false;
+    std::vector<double> zs(ma->cz, ma->cz + ne);
+    std::sort(zs.begin(), zs.end());
+    zs.erase(std::unique(zs.begin(), zs.end()), zs.end());
+    g.nZ = (int)zs.size();
+    g.iz.resize(ne);
+    for (int i = 0; i < ne; ++i) g.iz[i] = (int)(std::lower_bound(zs.begin(), zs.end(), ma->cz[i]) - zs.begin());
+    if ((long long)g.nX * g.nY * g.nZ != ne) return false;
+    g.cell.assign((size_t)ne, -1);  // (ix, iy, iz) -> cell, every slot exactly once
+    for (int i = 0; i < ne; ++i) {
+        int& c = g.cell[((size_t)g.iz[i] * g.nY + g.iy[i]) * g.nX + g.ix[i]];
+        if (c >= 0) return false;
+        c = i;
+    }
+    const long long keys = (2LL * g.nX - 1) * (2LL * g.nY - 1) * g.nZ * g.nZ;
+    return keys * 4 <= (long long)ne * ne;  // worth it only when keys are far fewer than pairs
+}
+
 int launch_gf_mm(const HexDev& m, double lambda, double mu, const double* qc, const double* qw, int nq,
-                 double* out, size_t ld, cudaStream_t s) {
+                 double* out, size_t ld, cudaStream_t s, const MMGrid* grid) {
     if (int rc = upload_gl_tables()) return rc;
     const long long total = (long long)m.ne * m.ne;
-    k_gf_mm<<<grid_for(total, 64), 64, 0, s>>>(m, lambda, mu, qc, qw, nq, out, ld);
+    if (!grid) {
+        k_gf_mm<<<grid_for(total, 64), 64, 0, s>>>(m, lambda, mu, qc, qw, nq, out, ld);
+        GBC_CUDA(cudaGetLastError());
+        return 0;
+    }
+    const MMGrid& g = *grid;
+    const long long nk = (2LL * g.nX - 1) * (2LL * g.nY - 1) * g.nZ * g.nZ;
+    std::vector<int2> reps((size_t)nk);
+    for (int dx = -(g.nX - 1); dx <= g.nX - 1; ++dx)
+        for (int dy = -(g.nY - 1); dy <= g.nY - 1; ++dy)
+            for (int zr = 0; zr < g.nZ; ++zr)
+                for (int zs = 0; zs < g.nZ; ++zs) {
+                    const int xs = std::max(0, -dx), ys = std::max(0, -dy);
+                    const long long key = (((long long)(dx + g.nX - 1) * (2 * g.nY - 1) + (dy + g.nY - 1)) * g.nZ + zr) * g.nZ + zs;
+                    const int jr = g.cell[((size_t)zr * g.nY + ys + dy) * g.nX + xs + dx];
+                    const int is = g.cell[((size_t)zs * g.nY + ys) * g.nX + xs];
+                    reps[(size_t)key] = make_int2(jr, is);
+                }
+    std::vector<int4> cells((size_t)m.ne);
+    for (int i = 0; i < m.ne; ++i) cells[(size_t)i] = make_int4(g.ix[i], g.iy[i], g.iz[i], 0);
+    int2* d_reps = nullptr;
+    int4* d_cells = nullptr;
+    double* d_table = nullptr;
+    GBC_CUDA(cudaMallocAsync(&d_reps, sizeof(int2) * nk, s));
+    GBC_CUDA(cudaMallocAsync(&d_cells, sizeof(int4) * m.ne, s));
+    GBC_CUDA(cudaMallocAsync(&d_table, sizeof(double) * 36 * nk, s));
+    GBC_CUDA(cudaMemcpyAsync(d_reps, reps.data(), sizeof(int2) * nk, cudaMemcpyHostToDevice, s));
+    GBC_CUDA(cudaMemcpyAsync(d_cells, cells.data(), sizeof(int4) * m.ne, cudaMemcpyHostToDevice, s));
+    k_gf_mm_keys<<<grid_for(nk, 64), 64, 0, s>>>(m, lambda, mu, qc, qw, nq, d_reps, nk, d_table);
     GBC_CUDA(cudaGetLastError());
+    k_gf_mm_expand<<<grid_for(total, 256), 256, 0, s>>>(m.ne, d_cells, g.nX, g.nY, g.nZ, d_table, out, ld);
+    GBC_CUDA(cudaGetLastError());
+    GBC_CUDA(cudaFreeAsync(d_reps, s));
+    GBC_CUDA(cudaFreeAsync(d_cells, s));
+    GBC_CUDA(cudaFreeAsync(d_table, s));
+    GBC_CUDA(cudaStreamSynchronize(s));  // the host vectors above must outlive the copies
     return 0;
 }
 

@@ -96,3 +96,27 @@ def test_invalid_buffer_ratio():
     mf = gen_mesh("RectOkada", 10.0, 10.0, 2.0, 2.0, 90.0)
     with pytest.raises(AssertionError):
         stress_greens_function(mf, 1.0, 1.0, buffer_ratio=-1.0)
+
+
+def test_gf_mm_structured_box_uses_offsets(oracle):
+    """A complete grid of equal cells takes the one-evaluation-per-(offset, layers) path: it matches the
+    oracle at the FP64-mode bar and the direct pair kernel (reached by moving one cell off the grid)
+    on every entry that does not involve the moved cell."""
+    import copy
+    from oetqf_gb300 import stress_greens_function
+    ma = gen_hex8_box(-30e3, -25e3, -10e3, 60e3, 50e3, -25e3, 6, 5, 3)   # 90 cells, 891 keys
+    g = stress_greens_function(ma, 3e10, 3e10)
+    c = oracle.gf_mm(ma, 3e10, 3e10)
+    _close(g, c, axis=1)
+    mb = copy.deepcopy(ma)
+    mb.cx = np.array(mb.cx, dtype=float)
+    mb.qx = np.array(mb.qx, dtype=float)
+    shift = 1e-7 * mb.Δx[0] if hasattr(mb, "Δx") else 1e-7 * np.asarray(mb.dx)[0]
+    mb.cx[0] += shift
+    mb.qx[0] += shift
+    gd = stress_greens_function(mb, 3e10, 3e10)
+    ne = ma.ne
+    keep_r = np.array([(r % ne) != 0 for r in range(6 * ne)])
+    keep_c = np.array([(c_ % ne) != 0 for c_ in range(6 * ne)])
+    a, b = g[np.ix_(keep_r, keep_c)], gd[np.ix_(keep_r, keep_c)]
+    np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-12 * np.abs(b).max())
