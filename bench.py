@@ -118,6 +118,21 @@ def dist():
     return tdist, tdist.get_rank(), ws
 
 
+def max_over_ranks(tdist, value: float, device: str) -> float:
+    """The slowest rank's time: every replica integrates its own model, so the job ends with the last."""
+    if tdist is None:
+        return value
+    import torch
+    t = torch.tensor([value], device=device, dtype=torch.float64)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world_size: int, sim_years_per_rank: float, ms_max: float) -> float:
+    """Whole-job sim-yr/s: every rank integrates its own replica over the same horizon."""
+    return world_size * sim_years_per_rank / (ms_max / 1e3)
+
+
 def cpu_oracle_model(cm, gfs=None):
     """The workload on the FP64 oracle. With gfs=None (no GPU on this path) the mantle Green's
     functions are stand-ins of the right shapes and scale: fault->mantle exact from the oracle,
@@ -247,12 +262,9 @@ def run_gpu(args):
     ms = e0.elapsed_time(e1)
     launches = C.kernel_launches() - launches0
     clk = clocks.stop()
-    if tdist:
-        t = torch.tensor([ms], device="cuda")
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(tdist, ms, "cuda")
     sim_yr = H / YEAR
-    value = ws * sim_yr / (ms / 1e3)
+    value = replica_throughput(ws, sim_yr, ms)
     # roofline of the dominant kernel (the row GEMV + friction launch): CUDA events on the model stream
     du = torch.zeros_like(u)
     R = 30
