@@ -548,7 +548,7 @@ def run_ensemble_profile(args):
 def run_serving(args):
     from oetqf_gb300.serving import Server, run_stream
     reqs = serving_requests(n_requests=args.requests)
-    s = Server(hbm_budget_gb=args.hbm_budget_gb)
+    s = Server(hbm_budget_gb=args.hbm_budget_gb, alg=args.alg)
     out = run_stream(s, reqs, rate_per_s=20.0, seed=1)
     info = s.info()
     s.close()
@@ -556,7 +556,8 @@ def run_serving(args):
     line = _base_line(out["sim_yr_per_s"], args, 1, {"workload": "serving-poisson-20rps", "requests": len(reqs),
                                                      "mantle_requests": sum(r.ma is not None for r in reqs),
                                                      "hbm_budget_gb": args.hbm_budget_gb, "peak_bytes": info.peak_bytes,
-                                                     "batch_iterations": info.iterations, "makespan_s": out["makespan_s"]},
+                                                     "batch_iterations": info.iterations, "makespan_s": out["makespan_s"],
+                                                     "solver": args.alg},
                       out["makespan_s"] * 1e3 / len(reqs), "f32+f64 / bf16")
     line["latency_s"] = {"p50": out["p50_s"], "p99": out["p99_s"], "max": float(lat.max())}
     line["gf_cache"] = {"hits": info.cache_hits, "misses": info.cache_misses, "resident_entries": info.cache_entries,

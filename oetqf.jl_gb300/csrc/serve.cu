@@ -7,7 +7,8 @@
 //    iteration boundaries or on the other requests (each model's step control state persists in
 //    its descriptor), so results are bitwise the same alone and in the mix.
 //  * Requests with a mantle run on their own model stream in a worker thread (block-scaled BF16
-//    Green's functions, ln θ state); their kernels overlap with the batch on the device.
+//    Green's functions; ln θ state under Tsit5, θ under VCABM5); their kernels overlap with the
+//    batch on the device.
 //  * Assembled Green's functions are cached on the device, keyed by the exact bytes of everything
 //    they depend on (mesh, elastic constants, fault type, images, buffer ratio, quadrature and
 //    storage precision): fault-only requests share one read-only spectrum buffer per geometry,
@@ -204,9 +205,13 @@ static int admit_fault(gbc_server* s, Req& r) {
                     std::make_pair(pboa, &boa), std::make_pair(piL, &iL)})
         if (e == cudaSuccess) e = up(pr.first, *pr.second);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (admission)");
-    k_theta_one<<<(int)((N + 255) / 256), 256, 0, st>>>(pu + N, (int)N, 1);
-    GBC_CUDA(cudaGetLastError());
-    count_launches(1);
+    // Tsit5 integrates ln θ; VCABM5 integrates θ itself
+    const int lt = (s->batch_opts.alg == GBC_ALG_VCABM5) ? 0 : 1;
+    if (lt) {
+        k_theta_one<<<(int)((N + 255) / 256), 256, 0, st>>>(pu + N, (int)N, 1);
+        GBC_CUDA(cudaGetLastError());
+        count_launches(1);
+    }
     GBC_CUDA(cudaStreamSynchronize(st));
     ge->valid = true;
     m.ghat = ge->ghat;
@@ -220,16 +225,18 @@ static int admit_fault(gbc_server* s, Req& r) {
     m.qold = 1e-4;
     m.maxiters = r.opts.maxiters;
     m.done = (r.t1 <= r.t0) ? 1 : 0;
-    m.log_theta = 1;
-    m.logged = 1;
+    m.log_theta = lt;
+    m.logged = lt;
     return 0;
 }
 
 static void finish_fault(gbc_server* s, Req& r) {
     const EnsModel& m = r.desc;
     const int N = m.N;
-    k_theta_one<<<(N + 255) / 256, 256, 0, s->batch>>>(m.u + N, N, 0);
-    count_launches(1);
+    if (m.logged) {
+        k_theta_one<<<(N + 255) / 256, 256, 0, s->batch>>>(m.u + N, N, 0);
+        count_launches(1);
+    }
     r.u1.resize(3 * (size_t)N);
     cudaMemcpyAsync(r.u1.data(), m.u, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s->batch);
     cudaFreeAsync(r.dmem, s->batch);
@@ -275,7 +282,7 @@ static void run_mantle(gbc_server* s, std::shared_ptr<Req> rp) {
     }
     if (!rc) rc = gbc_model_set_fault_props(m, r.a.data(), r.b.data(), r.L.data(), r.sig.data(), r.eta, r.vpl, r.f0, r.v0);
     if (!rc) rc = gbc_model_set_mantle_props(m, r.gamma.data(), r.nexp.data(), r.deps0);
-    if (!rc) rc = gbc_model_set_log_theta(m, r.precision != GBC_PREC_F64);
+    if (!rc) rc = gbc_model_set_log_theta(m, r.precision != GBC_PREC_F64 && r.opts.alg != GBC_ALG_VCABM5);
     r.u1 = r.u0;
     if (!rc) rc = gbc_integrate(m, r.u1.data(), r.t0, r.t1, &r.opts, &r.stats);
     std::lock_guard<std::mutex> lk(s->mu);
