@@ -40,7 +40,7 @@ SOLVER = dict(reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=0.2 * YEAR)
 # over the horizons the parity tests cover: 28543 and 12381 for the 800-patch fault, counted by
 # both); used to turn a bounded CPU sample into sim-yr/s.
 RHS_FOR_HORIZON = {("fault-mantle-1000x2500-f64", "Tsit5"): 6 * 42388 + 1,
-                   ("fault-mantle-1000x2500-f64", "VCABM5"): 138665,
+                   ("fault-mantle-1000x2500-f64", "VCABM5"): 138710,
                    ("fault-800-f64", "Tsit5"): 28543, ("fault-800-f64", "VCABM5"): 12381}
 WORKLOADS = ["fault-mantle-1000x2500-f64", "fault-800-f64"]
 # DRAM bytes (read + write) of one k_rows launch from ncu, per workload
