@@ -1,13 +1,17 @@
 // Batched ensemble: many independent fault-only cycle models of uneven size integrated in one
-// persistent launch, one CTA per model. Each CTA keeps its model's Toeplitz kernel (FP32) and the
-// slip-rate vector in shared memory and runs its own Tsit5 steps with its own dt (per-instance
-// step control); state, stage derivatives, the friction update and the error norm are FP64, the
-// traction-rate convolution accumulates in FP32. A launch runs at most `budget` steps per model
-// and returns; the host relaunches a captured CUDA graph of launches until every model is done.
+// persistent launch per cluster size, one CTA or one 2/4/8-CTA thread-block cluster per model. Each
+// model runs its own Tsit5 or VCABM5 steps with its own dt (per-instance step control). The
+// traction rate is an rFFT convolution in shared memory accumulating in FP32 (the spectra of the
+// circulant embedding of its Toeplitz kernel are precomputed per model); the state, stage sums,
+// friction update and error norm are FP64. Cluster ranks own whole 32-patch chunks and exchange
+// their slip rates and error-norm sums with st.async pushes into the peers' shared memory, so a
+// model's trajectory does not depend on the block or cluster size; as models finish, the host
+// moves the rest to larger clusters. A launch runs until its wall-clock budget and returns; the
+// host relaunches a captured CUDA graph until every model is done.
 //
 // Reference: the fault-only ode (src/BEM/equation.jl:156-166) = relative_velocity! (:35-42),
-// dτ_dt! (:44-61, applied as the direct Toeplitz sum), update_fault! (:233-246) and the ageing
-// law (:279); the integrator stands in for OrdinaryDiffEq's solve (src/io.jl:125-130).
+// dτ_dt! (:44-61, the FFT convolution), update_fault! (:233-246) and the ageing law (:279); the
+// integrators stand in for OrdinaryDiffEq's solve (src/io.jl:125-130).
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -728,7 +732,7 @@ int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtma
                    unsigned long long budget_ns, int block, size_t smem, cudaStream_t main, int alg) {
     EnsArgs A{};
     A.alg = alg;
-    A.models = L.models; A.nmodels = L.n; A.order = L.order; A.ctl = L.ctl;
+    A.models = L.models; A.nmodels = L.n; A.order = L.order;
     A.reltol = reltol; A.abstol = abstol; A.dtmax = dtmax; A.dtmin = dtmin;
     A.budget = 1 << 20;
     A.budget_ns = budget_ns;
@@ -759,7 +763,6 @@ int ens_launch_create(EnsLaunch& L, int capacity) {
     L = EnsLaunch();
     L.cap = capacity;
     GBC_CUDA(cudaMalloc(&L.order, sizeof(int) * capacity));
-    GBC_CUDA(cudaMalloc(&L.ctl, sizeof(int) * capacity));
     GBC_CUDA(cudaEventCreateWithFlags(&L.fork, cudaEventDisableTiming));
     for (int g = 0; g < 4; ++g) {
         GBC_CUDA(cudaStreamCreateWithFlags(&L.aux[g], cudaStreamNonBlocking));
@@ -770,7 +773,6 @@ int ens_launch_create(EnsLaunch& L, int capacity) {
 
 void ens_launch_destroy(EnsLaunch& L) {
     if (L.order) cudaFree((void*)L.order);
-    if (L.ctl) cudaFree(L.ctl);
     if (L.fork) cudaEventDestroy(L.fork);
     for (int g = 0; g < 4; ++g) {
         if (L.aux[g]) cudaStreamDestroy(L.aux[g]);

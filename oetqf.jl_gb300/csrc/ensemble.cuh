@@ -33,7 +33,6 @@ struct EnsArgs {
     int nmodels;
     const int* order;            // models of this launch, grouped by cluster size: order[first + i]
     int first;
-    int* ctl;
     int alg;                     // 0: Tsit5, 1: VCABM5                    // per model: stop flag of the current step (written by rank 0)
     double reltol, abstol, dtmax, dtmin;
     int budget;                      // step cap per launch and model
@@ -52,7 +51,6 @@ struct EnsLaunch {
     EnsModel* models = nullptr;
     int n = 0, cap = 0;
     const int* order = nullptr;  // device: model indices grouped by cluster size
-    int* ctl = nullptr;          // device: stop flags, one per model
     int first[4] = {0, 0, 0, 0}, count[4] = {0, 0, 0, 0};
     cudaStream_t aux[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t fork = nullptr, join[4] = {nullptr, nullptr, nullptr, nullptr};
