@@ -1,4 +1,4 @@
-// Device-resident adaptive Tsit5 integration of one model.
+// Device-resident adaptive integration of one model: Tsit5 or VCABM5.
 #pragma once
 #include <cuda_runtime.h>
 

@@ -8,7 +8,8 @@
 // Rows of the unified matrix: [0, M) mantle stress rates [G12 | 0 | G22] (equation.jl:202-203);
 // [Mpad, Mpad + N) the G21 part of the fault traction rate (equation.jl:201). The fault rows
 // then add the FP32 Toeplitz sum (equation.jl:44-61) and run the FP64 friction update
-// (equation.jl:233-246) in k_fault_rows_mixed.
+// (equation.jl:233-246) in k_fault_rows_smem (k_fault_rows_mixed for faults too large for its
+// shared-memory staging).
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
