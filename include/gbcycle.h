@@ -69,6 +69,11 @@ int gbc_stress_gf_mf(const gbc_hex_mesh* ma, const gbc_fault_mesh* mf, double la
  * out: (6ne, 6ne) column-major. */
 int gbc_stress_gf_mm(const gbc_hex_mesh* ma, double lambda, double mu, const double* qcoords,
                      const double* qweights, int nq, double* out);
+/* No reference counterpart: whether a mantle mesh is a complete grid of equal cells (centres on
+ * uniform x and y grids spaced by the cell size, any set of depths, equal source-corner offsets),
+ * which the mantle-mantle assembly evaluates once per (horizontal offset, layer pair) instead of
+ * once per cell pair. Returns 1 (and the grid size in nX, nY, nZ) or 0; host-only, no device use. */
+int gbc_hex_mesh_grid(const gbc_hex_mesh* ma, int* nX, int* nY, int* nZ);
 
 /* ---- Models: the ODEProblem parameter tuple of assemble (src/BEM/equation.jl:81-89,141-154) -- */
 

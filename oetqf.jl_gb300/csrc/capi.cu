@@ -399,6 +399,16 @@ int gbc_stress_gf_mf(const gbc_hex_mesh* ma, const gbc_fault_mesh* mf, double la
     return 0;
 }
 
+int gbc_hex_mesh_grid(const gbc_hex_mesh* ma, int* nX, int* nY, int* nZ) {
+    if (!ma || ma->ne <= 0) return 0;
+    MMGrid g;
+    if (!mm_grid(ma, g)) return 0;
+    if (nX) *nX = g.nX;
+    if (nY) *nY = g.nY;
+    if (nZ) *nZ = g.nZ;
+    return 1;
+}
+
 int gbc_stress_gf_mm(const gbc_hex_mesh* ma, double lambda, double mu, const double* qcoords,
                      const double* qweights, int nq, double* out) {
     if (int rc = check_device()) return rc;

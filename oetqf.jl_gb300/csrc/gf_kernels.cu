@@ -424,10 +424,15 @@ int launch_gf_mf(const HexDev& m, const FaultDev& f, double lambda, double mu, i
 bool mm_grid(const gbc_hex_mesh* ma, MMGrid& g) {
     const int ne = ma->ne;
     if (ne < 2) return false;
+    // equal within 1e-12 of the cell size (sizes and offsets computed from non-binary spacings
+    // differ in the last bits between cells); a pair then differs from its key's representative
+    // by a geometry change of that order
+    const double tol = 1e-12 * std::max(std::fabs(ma->dx[0]), std::max(std::fabs(ma->dy[0]), std::fabs(ma->dz[0])));
+    auto same = [&](double a, double b) { return std::fabs(a - b) <= tol; };
     for (int i = 0; i < ne; ++i)
-        if (ma->dx[i] != ma->dx[0] || ma->dy[i] != ma->dy[0] || ma->dz[i] != ma->dz[0] ||
-            ma->qx[i] - ma->cx[i] != ma->qx[0] - ma->cx[0] || ma->qy[i] - ma->cy[i] != ma->qy[0] - ma->cy[0] ||
-            ma->qz[i] - ma->cz[i] != ma->qz[0] - ma->cz[0])
+        if (!same(ma->dx[i], ma->dx[0]) || !same(ma->dy[i], ma->dy[0]) || !same(ma->dz[i], ma->dz[0]) ||
+            !same(ma->qx[i] - ma->cx[i], ma->qx[0] - ma->cx[0]) || !same(ma->qy[i] - ma->cy[i], ma->qy[0] - ma->cy[0]) ||
+            !same(ma->qz[i] - ma->cz[i], ma->qz[0] - ma->cz[0]))
             return false;
     auto axis = [&](const double* c, double d, std::vector<int>& idx, int& n) {
         double lo = c[0], hi = c[0];
@@ -445,10 +450,14 @@ bool mm_grid(const gbc_hex_mesh* ma, MMGrid& g) {
     if (!axis(ma->cx, ma->dx[0], g.ix, g.nX) || !axis(ma->cy, ma->dy[0], g.iy, g.nY)) return false;
     std::vector<double> zs(ma->cz, ma->cz + ne);
     std::sort(zs.begin(), zs.end());
-    zs.erase(std::unique(zs.begin(), zs.end()), zs.end());
+    zs.erase(std::unique(zs.begin(), zs.end(), [&](double a, double b) { return std::fabs(a - b) <= tol; }), zs.end());
     g.nZ = (int)zs.size();
     g.iz.resize(ne);
-    for (int i = 0; i < ne; ++i) g.iz[i] = (int)(std::lower_bound(zs.begin(), zs.end(), ma->cz[i]) - zs.begin());
+    for (int i = 0; i < ne; ++i) {
+        const auto it = std::lower_bound(zs.begin(), zs.end(), ma->cz[i] - tol);
+        if (it == zs.end() || std::fabs(*it - ma->cz[i]) > tol) return false;
+        g.iz[i] = (int)(it - zs.begin());
+    }
     if ((long long)g.nX * g.nY * g.nZ != ne) return false;
     g.cell.assign((size_t)ne, -1);  // (ix, iy, iz) -> cell, every slot exactly once
     for (int i = 0; i < ne; ++i) {

@@ -88,6 +88,7 @@ def lib():
             "gbc_ensemble_set_log_theta": [P, I],
             "gbc_ensemble_set_max_cluster": [P, I],
             "gbc_ensemble_set_regroup": [P, I],
+            "gbc_hex_mesh_grid": [ctypes.POINTER(HexMesh), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)],
             "gbc_ensemble_integrate": [P, PD, PD, PD, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
             "gbc_ensemble_integrate_dev": [P, P, PD, PD, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
         }
@@ -152,6 +153,16 @@ def fault_struct(mf, keep: Keep) -> FaultMesh:
 
 def hex_struct(ma, keep: Keep) -> HexMesh:
     return HexMesh(ma.ne, *(keep(getattr(ma, n)) for n in ("cx", "cy", "cz", "qx", "qy", "qz", "Δx", "Δy", "Δz")))
+
+
+def hex_mesh_grid(ma):
+    """(nX, nY, nZ) when the mesh is a complete grid of equal cells (the mantle-mantle assembly then
+    evaluates once per horizontal offset and layer pair), else None. Host-only."""
+    k = Keep()
+    h = hex_struct(ma, k)
+    nx, ny, nz = I(), I(), I()
+    ok = lib().gbc_hex_mesh_grid(ctypes.byref(h), ctypes.byref(nx), ctypes.byref(ny), ctypes.byref(nz))
+    return (nx.value, ny.value, nz.value) if ok else None
 
 
 def kernel_launches() -> int:

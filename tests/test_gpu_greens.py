@@ -114,6 +114,8 @@ def test_gf_mm_structured_box_uses_offsets(oracle):
     shift = 1e-7 * mb.Δx[0] if hasattr(mb, "Δx") else 1e-7 * np.asarray(mb.dx)[0]
     mb.cx[0] += shift
     mb.qx[0] += shift
+    from oetqf_gb300 import _capi as C
+    assert C.hex_mesh_grid(ma) == (6, 5, 3) and C.hex_mesh_grid(mb) is None  # the two paths are compared
     gd = stress_greens_function(mb, 3e10, 3e10)
     ne = ma.ne
     keep_r = np.array([(r % ne) != 0 for r in range(6 * ne)])
