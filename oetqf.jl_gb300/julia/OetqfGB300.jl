@@ -73,6 +73,23 @@ function set_props!(m::GB300Model, p::PowerLawViscosityProperty)
                 m.h, Vector{Float64}(p.γ), Vector{Float64}(p.n), Vector{Float64}(p.dϵ₀)))
 end
 
+"CompositePowerLawViscosityProperty (property.jl:43-48): the laws stacked law-major."
+function set_props!(m::GB300Model, p::CompositePowerLawViscosityProperty)
+    γ = reduce(vcat, (Vector{Float64}(q.γ) for q in p.piter))
+    n = reduce(vcat, (Vector{Float64}(q.n) for q in p.piter))
+    check(ccall((:gbc_model_set_mantle_props_composite, libgbc), Cint,
+                (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
+                m.h, length(p.piter), γ, n, Vector{Float64}(p.dϵ₀)))
+end
+
+"DilatancyProperty (property.jl:27-32) of a fault-only model; its state is (v, θ, δ, 𝓅)."
+function set_props!(m::GB300Model, p::DilatancyProperty)
+    check(ccall((:gbc_model_set_dilatancy, libgbc), Cint,
+                (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
+                m.h, Vector{Float64}(vec(p.tₚ)), Vector{Float64}(vec(p.ϵ)), Vector{Float64}(vec(p.β)),
+                Vector{Float64}(vec(p.p₀))))
+end
+
 "The drop-in derivative: OrdinaryDiffEq calls f(du, u, p, t) in place; u and du are ArrayPartitions."
 function gpu_ode(du::ArrayPartition, u::ArrayPartition, m::GB300Model, t)
     n = length(u.x)

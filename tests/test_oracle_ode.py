@@ -247,3 +247,28 @@ def test_vcabm5_matches_scipy(oracle):
     assert st.nrhs == 2 * st.naccept + st.nreject + 1  # PECE: two evaluations per accepted step
     ref = scipy_integrate.solve_ivp(lambda t, y: m.ode(y), (0.0, T), u0, method="DOP853", rtol=1e-12, atol=1e-16)
     np.testing.assert_allclose(u1, ref.y[:, -1], rtol=1e-7)
+
+
+def test_vcabm5_viscoelastic_matches_scipy(oracle):
+    """VCABM5 with a Maxwell mantle (state v, θ, ϵ, σ, δ) at tight tolerance against scipy DOP853."""
+    scipy_integrate = pytest.importorskip("scipy.integrate")
+    mf = gen_mesh("RectOkada", 8e3, 4e3, 1e3, 1e3, 90.0)
+    ma = gen_hex8_box(-4e3, -4e3, -6e3, 8e3, 8e3, -6e3, 2, 2, 2)
+    mu = 3e10
+    gfs = (oracle.gf_ff(mf, mu, mu, fourier=True), oracle.gf_fm(mf, ma, mu, mu), oracle.gf_mf(ma, mf, mu, mu),
+           oracle.gf_mm(ma, mu, mu))
+    N, ne = mf.nx * mf.nξ, ma.ne
+    o = np.ones((mf.nx, mf.nξ))
+    vpl = 1e-9
+    pf = RateStateQuasiDynamicProperty(0.015 * o, 0.019 * o, 0.012 * o, 5e7 * o, mu / (2 * 3044.0), vpl, 0.6, vpl)
+    pa = PowerLawViscosityProperty(np.full(ne, 5e-20), np.zeros(ne), np.zeros(6))
+    m = oracle.OracleModel(gfs[0], pf, *gfs[1:], pa)
+    th0 = 0.012 / vpl * (1 + 0.01 * np.linspace(-1, 1, N))
+    u0 = np.concatenate([np.full(N, vpl), th0, np.zeros(6 * ne), np.zeros(6 * ne), np.zeros(N)])
+    T = 3.15e7
+    u1, st = m.integrate(u0, 0.0, T, reltol=1e-10, abstol=1e-14, dt0=1e-3, alg="VCABM5")
+    assert st.status == 0 and st.t == T
+    ref = scipy_integrate.solve_ivp(lambda t, y: m.ode(y), (0.0, T), u0, method="DOP853", rtol=1e-12, atol=1e-16)
+    np.testing.assert_allclose(u1[:N], ref.y[:N, -1], rtol=1e-7)
+    np.testing.assert_allclose(u1[N:2 * N], ref.y[N:2 * N, -1], rtol=1e-7)
+    np.testing.assert_allclose(u1[2 * N + 6 * ne:], ref.y[2 * N + 6 * ne:, -1], rtol=1e-6, atol=1e-6 * np.abs(ref.y[2 * N + 6 * ne:, -1]).max())
