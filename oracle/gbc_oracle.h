@@ -2,7 +2,7 @@
  * CPU FP64 oracle for the earthquake-cycle hot path (Green's-function assembly + ODE right-hand
  * side + adaptive Runge-Kutta), restated from the reference Oetqf.jl v0.3.6.
  *
- * TEST INFRASTRUCTURE ONLY. This library is the checker for the CUDA path: only tests/,
+ * TEST INFRASTRUCTURE ONLY. This library is the FP64 reference the CUDA path is tested against: only tests/,
  * __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm may load it. The product
  * (libgbcycle.so) never links or calls it.
  *

@@ -2,7 +2,7 @@
  * Oracle: the four stress_greens_function methods of the reference (src/BEM/GF.jl) and the
  * Toeplitz -> rFFT embedding, restated loop for loop in C with OpenMP standing in for @threads.
  *
- * TEST INFRASTRUCTURE ONLY (the checker for the CUDA path; never linked into the product).
+ * TEST INFRASTRUCTURE ONLY (the FP64 reference the CUDA path is tested against; never linked into the product).
  */
 #include <math.h>
 #include <stdlib.h>

@@ -3,7 +3,7 @@
  * half-space -- the quantity GeoGreensFunctions.stress_vol_hex8! (Barbot, Moore & Lambert 2017,
  * BSSA 107(2)) returns at the reference's calls src/BEM/GF.jl:215-221 and :277-283.
  *
- * TEST INFRASTRUCTURE ONLY (the checker for the CUDA path; never linked into the product).
+ * TEST INFRASTRUCTURE ONLY (the FP64 reference the CUDA path is tested against; never linked into the product).
  *
  * Method (not Barbot's closed form, which is not available here): a uniform eigenstrain
  * eps*_ij in a volume equals a continuous stack of planar Volterra dislocations whose slip per

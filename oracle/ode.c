@@ -2,7 +2,7 @@
  * Oracle: the ODE right-hand sides of src/BEM/equation.jl and an adaptive Tsit5 integrator
  * standing in for the reference's OrdinaryDiffEq caller.
  *
- * TEST INFRASTRUCTURE ONLY (the checker for the CUDA path, and the timed CPU baseline; never
+ * TEST INFRASTRUCTURE ONLY (the FP64 reference the CUDA path is tested against, and the timed CPU baseline; never
  * linked into the product).
  *
  * The fault-fault traction rate is computed as the reference does it (equation.jl:44-61): a real

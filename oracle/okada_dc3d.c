@@ -3,7 +3,7 @@
  * half-space (BSSA 82(2), 1018-1040), the arithmetic behind GeoGreensFunctions.dc3d that the
  * reference calls at src/BEM/GF.jl:49-53 and :156-160 (dc3d_cache at :43,:142).
  *
- * TEST INFRASTRUCTURE ONLY (the checker for the CUDA path; never linked into the product).
+ * TEST INFRASTRUCTURE ONLY (the FP64 reference the CUDA path is tested against; never linked into the product).
  *
  * Written from the paper's decomposition u = uA(image) - uA(real) + uB + z uC with Chinnery's
  * corner notation. The displacement formulas per corner are evaluated on forward-mode dual

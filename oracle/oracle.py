@@ -1,6 +1,6 @@
 """ctypes front end of the CPU FP64 oracle (oracle/*.c).
 
-TEST INFRASTRUCTURE ONLY: the checker for the CUDA path. Only tests/, __graft_entry__.smoke()
+TEST INFRASTRUCTURE ONLY: the FP64 reference the CUDA path is tested against. Only tests/, __graft_entry__.smoke()
 and bench.py's CPU-baseline / reference arm import this module; the product never does.
 
 Parity status: the Okada/strain-volume values are "parity unpinned" against the reference

@@ -16,7 +16,7 @@ def test_rect_okada():
     assert msh.x[-1] - msh.x[0] == pytest.approx(msh.Δx * (msh.nx - 1), rel=1e-15)
 
 
-def test_rect_okada_configs():
+def test_rect_okada_shapes():
     m0 = gen_mesh("RectOkada", 80e3, 10e3, 1e3, 1e3, 90.0)
     assert (m0.nx, m0.nξ) == (80, 10)
     assert m0.ξ[0] == -500.0 and m0.aξ[0][1] == 0.0 and m0.z[-1] == -9500.0
