@@ -28,8 +28,9 @@ def _ftype(ftype) -> int:
 def _quad(qtype):
     if qtype is None or (isinstance(qtype, str) and qtype == "Gauss1"):
         return np.zeros(3), np.ones(1)
-    if isinstance(qtype, str):
-        raise ValueError(f"quadrature {qtype!r} needs explicit (coords, weights); only 'Gauss1' is built in")
+    if isinstance(qtype, str):  # "GaussN": the hexahedron rule, weights normalised (GF.jl:318-323)
+        from .mesh import get_quadrature
+        qtype = get_quadrature(qtype)
     coords, weights = (np.asarray(q, dtype=np.float64).reshape(-1) for q in qtype)
     if len(coords) != 3 * len(weights):
         raise AssertionError("Wrong format of quadrature!")

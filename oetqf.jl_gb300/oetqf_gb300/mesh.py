@@ -146,3 +146,30 @@ def gauss_product_quadrature(order: int):
                 wts.append(w[i] * w[j] * w[k])
     wts = np.asarray(wts)
     return np.asarray(pts), wts / wts.sum()
+
+
+def gmsh_quadrature(etype: int, qtype: str):
+    """gmsh_quadrature(etype, qtype) (src/BEM/GF.jl:300-316) for the hexahedron (Gmsh element type 5):
+    the tensor-product Gauss-Legendre rule that integrates polynomials of the order named by
+    "GaussN" exactly (ceil((N+1)/2) points per direction, as Gmsh builds it since 4.9), local
+    coordinates on [-1, 1]^3 flattened (x, y, z) per point, weights summing to the element volume 8.
+    Gmsh itself is not needed: only this element is on the path."""
+    if etype != 5:
+        raise NotImplementedError("only the 8-node hexahedron (Gmsh element type 5) is on this path")
+    if not (isinstance(qtype, str) and qtype.startswith("Gauss") and qtype[5:].isdigit()):
+        raise ValueError(f"unknown quadrature {qtype!r} (expected 'GaussN')")
+    order = int(qtype[5:])
+    n = max(1, (order + 2) // 2)
+    coords, w = gauss_product_quadrature(n)
+    return coords, w * 8.0
+
+
+def get_quadrature(qtype):
+    """get_quadrature (src/BEM/GF.jl:318-328): a "GaussN" name gives the hexahedron rule with
+    weights normalised to sum 1; an explicit (coords, weights) tuple is checked and passed on."""
+    if isinstance(qtype, str):
+        c, w = gmsh_quadrature(5, qtype)
+        return c, w / w.sum()
+    coords, weights = qtype
+    assert len(np.ravel(coords)) == 3 * len(np.ravel(weights)), "Wrong format of quadrature!"
+    return qtype

@@ -47,3 +47,27 @@ def test_hex8_box_layers():
     me = gen_hex8_box(-40e3, -2.5e3, -8e3, 80e3, 5e3, -22e3, 4, 3, 3, rfzh=np.cumprod(np.ones(3) * 1.5))
     assert me.ne == 36
     np.testing.assert_allclose(np.sort(np.unique(np.round(me.Δz, 6))), np.sort(22e3 * np.array([1.5, 2.25, 3.375]) / 7.125))
+
+
+def test_gmsh_quadrature_hex():
+    """gmsh_quadrature(5, "GaussN") / get_quadrature (src/BEM/GF.jl:300-328): tensor-product rules that
+    integrate monomials of total degree <= N exactly over [-1, 1]^3; get_quadrature normalises."""
+    from oetqf_gb300 import get_quadrature, gmsh_quadrature
+    for order in (1, 2, 3, 4, 5):
+        c, w = gmsh_quadrature(5, f"Gauss{order}")
+        pts = np.asarray(c).reshape(-1, 3)
+        assert pts.shape[0] == len(w) and abs(w.sum() - 8.0) < 1e-13
+        for a in range(order + 1):
+            for b in range(order + 1 - a):
+                for d in range(order + 1 - a - b):
+                    exact = np.prod([0.0 if k % 2 else 2.0 / (k + 1) for k in (a, b, d)])
+                    got = np.sum(w * pts[:, 0] ** a * pts[:, 1] ** b * pts[:, 2] ** d)
+                    assert abs(got - exact) < 1e-12
+        cn, wn = get_quadrature(f"Gauss{order}")
+        assert abs(wn.sum() - 1.0) < 1e-14
+    c1, w1 = get_quadrature("Gauss1")
+    np.testing.assert_array_equal(np.asarray(c1).reshape(-1), np.zeros(3))
+    with pytest.raises(NotImplementedError):
+        gmsh_quadrature(4, "Gauss1")
+    with pytest.raises(AssertionError):
+        get_quadrature((np.zeros(4), np.ones(2)))
