@@ -493,22 +493,30 @@ int launch_gf_mm(const HexDev& m, double lambda, double mu, const double* qc, co
                 }
     std::vector<int4> cells((size_t)m.ne);
     for (int i = 0; i < m.ne; ++i) cells[(size_t)i] = make_int4(g.ix[i], g.iy[i], g.iz[i], 0);
-    int2* d_reps = nullptr;
-    int4* d_cells = nullptr;
-    double* d_table = nullptr;
-    GBC_CUDA(cudaMallocAsync(&d_reps, sizeof(int2) * nk, s));
-    GBC_CUDA(cudaMallocAsync(&d_cells, sizeof(int4) * m.ne, s));
-    GBC_CUDA(cudaMallocAsync(&d_table, sizeof(double) * 36 * nk, s));
-    GBC_CUDA(cudaMemcpyAsync(d_reps, reps.data(), sizeof(int2) * nk, cudaMemcpyHostToDevice, s));
-    GBC_CUDA(cudaMemcpyAsync(d_cells, cells.data(), sizeof(int4) * m.ne, cudaMemcpyHostToDevice, s));
-    k_gf_mm_keys<<<grid_for(nk, 64), 64, 0, s>>>(m, lambda, mu, qc, qw, nq, d_reps, nk, d_table);
+    // temporaries freed on every path; the stream is drained before the host vectors go away
+    struct Tmp {
+        int2* reps = nullptr;
+        int4* cells = nullptr;
+        double* table = nullptr;
+        cudaStream_t s;
+        ~Tmp() {
+            cudaStreamSynchronize(s);
+            if (reps) cudaFree(reps);
+            if (cells) cudaFree(cells);
+            if (table) cudaFree(table);
+        }
+    } t;
+    t.s = s;
+    GBC_CUDA(cudaMalloc(&t.reps, sizeof(int2) * nk));
+    GBC_CUDA(cudaMalloc(&t.cells, sizeof(int4) * m.ne));
+    GBC_CUDA(cudaMalloc(&t.table, sizeof(double) * 36 * nk));
+    GBC_CUDA(cudaMemcpyAsync(t.reps, reps.data(), sizeof(int2) * nk, cudaMemcpyHostToDevice, s));
+    GBC_CUDA(cudaMemcpyAsync(t.cells, cells.data(), sizeof(int4) * m.ne, cudaMemcpyHostToDevice, s));
+    k_gf_mm_keys<<<grid_for(nk, 64), 64, 0, s>>>(m, lambda, mu, qc, qw, nq, t.reps, nk, t.table);
     GBC_CUDA(cudaGetLastError());
-    k_gf_mm_expand<<<grid_for(total, 256), 256, 0, s>>>(m.ne, d_cells, g.nX, g.nY, g.nZ, d_table, out, ld);
+    k_gf_mm_expand<<<grid_for(total, 256), 256, 0, s>>>(m.ne, t.cells, g.nX, g.nY, g.nZ, t.table, out, ld);
     GBC_CUDA(cudaGetLastError());
-    GBC_CUDA(cudaFreeAsync(d_reps, s));
-    GBC_CUDA(cudaFreeAsync(d_cells, s));
-    GBC_CUDA(cudaFreeAsync(d_table, s));
-    GBC_CUDA(cudaStreamSynchronize(s));  // the host vectors above must outlive the copies
+    GBC_CUDA(cudaStreamSynchronize(s));
     return 0;
 }
 
