@@ -170,8 +170,14 @@ static int admit_fault(gbc_server* s, Req& r) {
         return cudaMemcpyAsync(dd, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, st);
     };
     if (!ge->valid) {  // first request of this geometry: its spectra, from a transient FP64 kernel
-        double* tmp = nullptr;
-        GBC_CUDA(cudaMallocAsync(&tmp, sizeof(double) * (nst + 3 * (size_t)r.nx + 4 * (size_t)r.nxi), st));
+        struct Tmp {  // released on every path, after the stream's work on it
+            double* p = nullptr;
+            cudaStream_t s;
+            ~Tmp() { if (p) cudaFreeAsync(p, s); }
+        } tg;
+        tg.s = st;
+        GBC_CUDA(cudaMallocAsync(&tg.p, sizeof(double) * (nst + 3 * (size_t)r.nx + 4 * (size_t)r.nxi), st));
+        double* tmp = tg.p;
         GBC_CUDA(cudaMallocAsync(&ge->ghat, sizeof(float) * ng, st));
         double* mx = tmp + nst;  // mesh: x (nx), y, z (nxi), ax (2nx), axi (2nxi)
         double *my = mx + r.nx, *mz = my + r.nxi, *max_ = mz + r.nxi, *maxi = max_ + 2 * r.nx;
@@ -184,7 +190,6 @@ static int admit_fault(gbc_server* s, Req& r) {
         if (int rc = launch_gf_ff(f, r.lambda, r.mu, r.ftype, r.nrept, r.buffer_ratio, tmp, st)) return rc;
         if (int rc = ens_ghat(tmp, m, ge->ghat, st)) return rc;
         count_launches(2);
-        GBC_CUDA(cudaFreeAsync(tmp, st));
     }
     GBC_CUDA(cudaMallocAsync(&r.dmem, sizeof(double) * 37 * N + 256, st));
     double* pa = static_cast<double*>(r.dmem);
