@@ -11,6 +11,7 @@
  * DFT is the direct O(n^2) sum with tabulated twiddles (FFTW is not available here).
  */
 #include <math.h>
+#include <omp.h>
 #include <stdlib.h>
 #include <string.h>
 #include "gbc_oracle.h"
@@ -31,20 +32,26 @@ static void tw_get(int n) {
 void orc_dtau_dt(const orc_model* m, const double* v, double* dtau) {
     const int nx = m->nx, nxi = m->nxi, n = 2 * nx - 1;
     tw_get(n);
+    const double* cs = tw.cs;  /* the calling thread's tables (they are thread-local) */
+    const double* sn = tw.sn;
     double* X = (double*)malloc(sizeof(double) * 2 * nx * nxi);   /* relv_dft (nx,nxi) complex */
     double* Y = (double*)calloc(2 * (size_t)nx * nxi, sizeof(double)); /* dtau_dft */
+    /* every output element is summed by one thread in a fixed order: results do not depend on the
+     * thread count */
+#pragma omp parallel for schedule(static)
     for (int l = 0; l < nxi; ++l)
         for (int k = 0; k < nx; ++k) {
             double re = 0.0, im = 0.0;
             for (int r = 0; r < nx; ++r) {
                 double val = v[r + nx * l] - m->vpl;
                 int idx = (int)(((long long)k * r) % n);
-                re += val * tw.cs[idx];
-                im -= val * tw.sn[idx];
+                re += val * cs[idx];
+                im -= val * sn[idx];
             }
             X[2 * (k + nx * l)] = re;
             X[2 * (k + nx * l) + 1] = im;
         }
+#pragma omp parallel for schedule(static)
     for (int j = 0; j < nxi; ++j)
         for (int l = 0; l < nxi; ++l)
             for (int k = 0; k < nx; ++k) {
@@ -54,13 +61,14 @@ void orc_dtau_dt(const orc_model* m, const double* v, double* dtau) {
                 y[0] += g[0] * x[0] - g[1] * x[1];
                 y[1] += g[0] * x[1] + g[1] * x[0];
             }
+#pragma omp parallel for schedule(static)
     for (int j = 0; j < nxi; ++j)
         for (int r = 0; r < nx; ++r) {
             double acc = Y[2 * (nx * j)];
             for (int k = 1; k < nx; ++k) {
                 int idx = (int)(((long long)k * r) % n);
                 const double* y = Y + 2 * (k + nx * j);
-                acc += 2.0 * (y[0] * tw.cs[idx] - y[1] * tw.sn[idx]);
+                acc += 2.0 * (y[0] * cs[idx] - y[1] * sn[idx]);
             }
             dtau[r + nx * j] = acc / n;
         }
@@ -93,8 +101,16 @@ void orc_ode_fault(const orc_model* m, const double* v, const double* th, double
 }
 
 /* y (+)= A x for column-major A (rows x cols); rows split across threads */
+/* y (+)= A x for a column-major A: row blocks in parallel, each row summing its columns in order
+ * (the result does not depend on the blocking). Short matrices (the 1000-row mantle->fault block
+ * of a 1000-patch fault) get thinner blocks so that every thread streams a part. */
 static void gemv_cm(const double* A, size_t rows, size_t cols, const double* x, double* y, int accumulate) {
-    const size_t B = 512;
+    const size_t nt = (size_t)omp_get_max_threads();
+    size_t B = 512;  /* 4 KB of a column per block: long contiguous runs for the tall blocks */
+    if ((rows + B - 1) / B < nt) {
+        B = (rows + nt - 1) / nt;
+        B = B < 32 ? 32 : (B + 7) / 8 * 8;
+    }
     const long nb = (long)((rows + B - 1) / B);
 #pragma omp parallel for schedule(static)
     for (long bi = 0; bi < nb; ++bi) {
