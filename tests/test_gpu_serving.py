@@ -15,15 +15,16 @@ def _mix():
     return reqs
 
 
-def test_alone_equals_in_the_mix():
+@pytest.mark.parametrize("alg", ["Tsit5", "VCABM5"])
+def test_alone_equals_in_the_mix(alg):
     from oetqf_gb300.serving import Server, run_stream
     reqs = _mix()
-    s = Server(hbm_budget_gb=8.0)
+    s = Server(hbm_budget_gb=8.0, alg=alg)
     out = run_stream(s, reqs, rate_per_s=50.0, seed=1)
     s.close()
     assert out["status"] == [0]
     for i in (0, 1, 2, 3, 4, 5):
-        alone = Server(hbm_budget_gb=8.0)
+        alone = Server(hbm_budget_gb=8.0, alg=alg)
         rid = alone.submit(reqs[i])
         u_alone, res = alone.wait(rid)
         alone.close()
