@@ -445,6 +445,94 @@ def run_mixed_large(args):
     print(json.dumps(line), flush=True)
 
 
+def run_sweep(args):
+    """Property variants of the 4096-patch + 8000-cell model sharing its block-scaled BF16 Green's
+    functions (gbc_sweep): aggregate sim-yr/s over a window against the single-model BF16 path."""
+    import torch
+    from oetqf_gb300 import _capi as C
+    from oetqf_gb300.equation import GB300Model
+    from oetqf_gb300.property import PowerLawViscosityProperty, RateStateQuasiDynamicProperty
+    from oetqf_gb300.sweep import Sweep
+    cm = large_fault_with_mantle()
+    years = args.years or 20.0
+    K = args.variants
+    m = GB300Model(cm.mf.nx, cm.mf.nξ, cm.ne)
+    m.assemble_gf(cm.mf, cm.ma, cm.lam, cm.mu)
+    m.set_fault_props(cm.pf)
+    m.set_mantle_props(cm.pa)
+    m.set_precision(C.GBC_PREC_BF16)
+    N, E = cm.N, 6 * cm.ne
+    props, u0s = [], []
+    for k in range(K):  # normal stress, state distance and mantle viscosity vary across the variants
+        s_k, l_k = 1.0 + 0.05 * k, 1.0 + 0.1 * k
+        pf = RateStateQuasiDynamicProperty(cm.pf.a, cm.pf.b, cm.pf.L * l_k, cm.pf.σ * s_k, cm.pf.η, cm.pf.vpl,
+                                           cm.pf.f0, cm.pf.v0)
+        pa = PowerLawViscosityProperty(cm.pa.γ * (1.0 + 0.25 * k), cm.pa.n, cm.pa.dϵ0)
+        u = cm.u0.copy()
+        u[N:2 * N] *= l_k
+        props.append((pf, pa))
+        u0s.append(u)
+    sw = Sweep(m, K, engine=args.engine)
+    for k, (pf, pa) in enumerate(props):
+        sw.set_fault_props(k, pf)
+        sw.set_mantle_props(k, pa)
+    stream = torch.cuda.ExternalStream(sw.stream)
+    U = torch.tensor(np.stack(u0s), device="cuda")
+    DU = torch.zeros_like(U)
+    for _ in range(max(args.warmup, 3)):
+        sw.rhs_dev(U.data_ptr(), DU.data_ptr())
+    r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    r0.record(stream)
+    for _ in range(20):
+        sw.rhs_dev(U.data_ptr(), DU.data_ptr())
+    r1.record(stream)
+    r1.synchronize()
+    rhs_ms = r0.elapsed_time(r1) / 20
+    edges = np.linspace(0.0, years * YEAR, args.steps + 1)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    steps = np.zeros(K, dtype=np.int64)
+    for i in range(args.steps):
+        st = sw.integrate_dev(U.data_ptr(), float(edges[i]), float(edges[i + 1]), alg=args.alg, **SOLVER)
+        steps += np.array([s.naccept + s.nreject for s in st])
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    assert sw.error_word() == 0
+    # the single-model BF16 path on variant 0 (the base's own properties) over the same window
+    stream1 = torch.cuda.ExternalStream(m.stream)
+    u = torch.tensor(u0s[0], device="cuda")
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream1)
+    for i in range(args.steps):
+        m.integrate_dev(u.data_ptr(), float(edges[i]), float(edges[i + 1]), alg=args.alg, **SOLVER)
+    f1.record(stream1)
+    f1.synchronize()
+    ms1 = f0.elapsed_time(f1)
+    v_sw, v_1 = U[0, :N].cpu().numpy(), u[:N].cpu().numpy()
+    err = float(np.abs(v_sw - v_1).max() / np.abs(v_1).max())
+    matrix_bytes = (E * (N + E) + N * E) * 2
+    reads = 1 if args.engine == "umma" else (K + 7) // 8
+    peak = _peak()
+    ach = matrix_bytes * reads / (rhs_ms / 1e3) / 1e9
+    line = _base_line(K * years / (ms / 1e3), args, 1,
+                      {"workload": f"sweep-4096x8000-bf16-K{K}", "variants": K, "engine": args.engine,
+                       "fault_patches": N, "mantle_cells": cm.ne, "window_yr": years, "solver": args.alg,
+                       "rk_steps_per_variant": [int(x) for x in steps],
+                       "variants_differ_in": "normal stress (+5%/variant), state distance L (+10%), mantle viscosity (+25%)",
+                       "storage": "BF16 with FP32 scale per 128x128 block shared by all variants; FP32 Toeplitz; FP64 friction, theta state",
+                       "l2": "inputs larger than L2"}, ms / args.steps, "bf16")
+    line["roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                        "traffic": None, "kernel": f"k_sw_gemm_{args.engine} + k_sw_prologue + k_sw_fault_rows (one RHS of all variants)",
+                        "rhs_ms": rhs_ms, "bytes_per_launch": matrix_bytes * reads}
+    line["single_model"] = {"value": years / (ms1 / 1e3), "unit": "sim-yr/s"}
+    line["speedup_vs_single_model"] = line["value"] / line["single_model"]["value"]
+    line["variant0_max_slip_rate_rel_diff_vs_single_model"] = err
+    print(json.dumps(line), flush=True)
+
+
 def run_ensemble(args):
     """256 fault-only models of uneven size in one persistent launch vs the plain FP64 GPU path."""
     import torch
@@ -574,7 +662,7 @@ def main():
     ap.add_argument("--impl", default="gbcycle", choices=["gbcycle", "reference"])
     ap.add_argument("--workload", default="fault-mantle-1000x2500-f64",
                     choices=WORKLOADS + ["fault-mantle-4096x8000-mixed", "ensemble-256", "serving",
-                                                       "ensemble-profile"])
+                                                       "ensemble-profile", "sweep-4096x8000"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "f16"])
     ap.add_argument("--alg", default=None, choices=["VCABM5", "Tsit5"],
                     help="integrator (default: VCABM5, the reference example's solver; with it the state holds θ; "
@@ -587,6 +675,8 @@ def main():
     ap.add_argument("--profile-rhs", type=int, default=0, help="run N right-hand sides only (for ncu captures)")
     ap.add_argument("--years", type=float, default=0.0, help="override the horizon (profiling runs only)")
     ap.add_argument("--profile-precision", default="f64", choices=["f64", "bf16", "f16", "df64"])
+    ap.add_argument("--variants", type=int, default=8, help="property variants of the sweep workload")
+    ap.add_argument("--engine", default="simt", choices=["simt", "umma"], help="product engine of the sweep workload")
     ap.add_argument("--storage", default="f64", choices=["f64", "df64"],
                     help="mantle Green's functions of the fault-mantle workloads: FP64, or FP32 pairs (FP64-accurate)")
     args = ap.parse_args()
@@ -602,6 +692,8 @@ def main():
         run_ensemble_profile(args)
     elif args.workload == "serving":
         run_serving(args)
+    elif args.workload == "sweep-4096x8000":
+        run_sweep(args)
     else:
         run_gpu(args)
 

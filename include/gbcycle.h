@@ -248,6 +248,49 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
                                const gbc_solver_opts* opts, gbc_solver_stats* stats);
 void* gbc_ensemble_stream(gbc_ensemble* e);
 
+/* ---- Parameter sweeps on one geometry (tensor-core batched right-hand side) ------------------ */
+
+typedef struct gbc_sweep gbc_sweep;
+
+#define GBC_SWEEP_SIMT 0  /* product on the FP32 pipe, each variant's sums in the single model's order
+                             (the default) */
+#define GBC_SWEEP_UMMA 1  /* product on the tensor cores (tcgen05, BF16 x BF16 -> FP32) */
+
+/* nvariants (1..64) copies of a viscoelastic model's ODE (equation.jl:185-205) that share the base
+ * model's Green's functions and differ in properties and state -- the reference's way of rerunning
+ * one assembled model with other properties (examples/otf-with-mantle.jl:44-56, 140-162) batched on
+ * the device. The base model must use GBC_PREC_BF16 with its Green's functions and properties set;
+ * each variant starts with the base's properties. One right-hand side applies the block-scaled
+ * mantle rows to every variant's state at once: a product with nvariants columns that reads the
+ * matrix once. The base must outlive the sweep and keep its Green's functions and precision (the
+ * sweep fails with GBC_ESTATE otherwise); the fault must satisfy N + nx*nxi <= 40960. */
+int gbc_sweep_create(gbc_model* base, int nvariants, gbc_sweep** out);
+void gbc_sweep_destroy(gbc_sweep* s);
+/* Properties of variant k (same meaning as gbc_model_set_fault_props / _mantle_props; gamma and n
+ * have the base's number of power laws, law-major). */
+int gbc_sweep_set_fault_props(gbc_sweep* s, int k, const double* a, const double* b, const double* L,
+                              const double* sigma, double eta, double vpl, double f0, double v0);
+int gbc_sweep_set_mantle_props(gbc_sweep* s, int k, const double* gamma, const double* n,
+                               const double* deps0);
+/* GBC_SWEEP_SIMT (default) or GBC_SWEEP_UMMA. */
+int gbc_sweep_set_engine(gbc_sweep* s, int engine);
+/* State length of one variant; states are variant-major (variant k at k * gbc_sweep_state_len). */
+long long gbc_sweep_state_len(const gbc_sweep* s);
+/* ode(du, u, p, t) for every variant: u, du hold nvariants flat states (host, or device for _dev,
+ * which runs on the sweep's stream without synchronising). */
+int gbc_sweep_rhs(gbc_sweep* s, const double* u, double* du);
+int gbc_sweep_rhs_dev(gbc_sweep* s, const double* u, double* du);
+/* Integrates every variant from t0 to t1 with its own step control (opts->alg: Tsit5 or VCABM5);
+ * stats has nvariants entries. The variants share each right-hand side evaluation; a variant that
+ * reached t1 stops changing while the others continue. */
+int gbc_sweep_integrate(gbc_sweep* s, double* u, double t0, double t1, const gbc_solver_opts* opts,
+                        gbc_solver_stats* stats);
+int gbc_sweep_integrate_dev(gbc_sweep* s, double* u_dev, double t0, double t1,
+                            const gbc_solver_opts* opts, gbc_solver_stats* stats);
+/* Device error word of the tensor-core pipeline's bounded waits (0 = none). */
+int gbc_sweep_error_word(gbc_sweep* s);
+void* gbc_sweep_stream(gbc_sweep* s);
+
 /* ---- Serving: continuous batching of cycle-simulation requests on one GPU ------------------ */
 
 typedef struct gbc_server gbc_server;

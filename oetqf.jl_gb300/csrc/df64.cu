@@ -89,26 +89,10 @@ int split_mantle(int nx, int nxi, int npad, long long M, long long Mpad, long lo
 }
 
 int encode_pairmap(void* q, long long rowsq, long long ldq, void* tmap_out) {
-    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-    if (!encode) {
-        cudaDriverEntryPointQueryResult qr;
-        void* fn = nullptr;
-        GBC_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr));
-        if (qr != cudaDriverEntryPointSuccess || !fn) return fail(GBC_ECUDA, "cuTensorMapEncodeTiled unavailable");
-        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-    }
     // the pair matrix seen as 8-byte elements (one FP32 pair each; TMA only moves the bytes): the
     // inner box is 256 pairs = 2 KB, every tile starts at a multiple of 2 KB (16-byte TMA rule)
     // and the row stride is 8*ldq bytes
-    const cuuint64_t dims[2] = {(cuuint64_t)ldq, (cuuint64_t)rowsq};
-    const cuuint64_t strides[1] = {(cuuint64_t)ldq * 8};
-    const cuuint32_t box[2] = {DC, DR};
-    const cuuint32_t estr[2] = {1, 1};
-    CUresult r = encode(static_cast<CUtensorMap*>(tmap_out), CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, q, dims, strides, box,
-                        estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(GBC_ECUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
-    return 0;
+    return encode_tmap_2d(q, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, rowsq, ldq, DC, DR, false, tmap_out);
 }
 
 // ---- compensated arithmetic -----------------------------------------------------------------

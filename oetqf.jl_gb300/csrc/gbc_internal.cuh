@@ -27,6 +27,15 @@ int sm_count();
 // device; thread-safe, set once per kernel, device and size)
 int set_smem_limit(const void* fn, int bytes);
 
+// adds n to the library's kernel-launch counter (gbc_kernel_launches)
+void count_launches(long long n);
+
+// 2-D tiled TMA descriptor (CUtensorMap, 128 bytes at tmap_out) over a row-major rows x cols array
+// of esize-byte elements of CUtensorMapDataType dtype, box box_rows x box_cols; swizzle128 selects
+// the 128-byte swizzle (box_cols * esize must then be 128)
+int encode_tmap_2d(void* base, int dtype, int esize, long long rows, long long cols, int box_cols, int box_rows,
+                   bool swizzle128, void* tmap_out);
+
 // Gauss-Legendre tables for the strain-volume stacks (4, 8, 12, 16 nodes), in constant memory.
 void gl_rule(int n, double* x, double* w);
 int upload_gl_tables();

@@ -52,6 +52,26 @@ struct Integrator {
     double* phi[6] = {};  // VCABM: modified divided differences Phi_0..Phi_5 (allocated on first use)
 };
 
+// Ctrl at the start of an integration from t0 to t1 (VCABM5 starts at order 1; done when t1 <= t0)
+inline Ctrl ctrl_start(int alg, double t0, double t1, double reltol, double abstol, double dt0, double dtmax,
+                       double dtmin, long long maxiters) {
+    Ctrl h{};
+    h.alg = alg;
+    h.k = 1;
+    h.t = t0;
+    h.t1 = t1;
+    h.dt = dt0 < dtmax ? dt0 : dtmax;
+    if (h.dt > t1 - t0) h.dt = t1 - t0;
+    h.qold = 1e-4;
+    h.reltol = reltol;
+    h.abstol = abstol;
+    h.dtmax = dtmax;
+    h.dtmin = dtmin;
+    h.maxiters = maxiters;
+    h.done = (t1 <= t0) ? 1 : 0;
+    return h;
+}
+
 int integrator_alloc(Integrator& I, long long n);
 void integrator_free(Integrator& I);
 // Integrates u (device) from t0 to t1 with Tsit5 (alg 0) or VCABM5 (alg 1). Fills the host mirror

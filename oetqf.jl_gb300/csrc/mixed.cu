@@ -19,6 +19,7 @@
 #include <cstring>
 
 #include "gbc_internal.cuh"
+#include "mixed.cuh"
 #include "rhs.cuh"
 #include "tma.cuh"
 
@@ -109,7 +110,8 @@ int fault_f32(const double* st, float* st32, long long n, cudaStream_t s) {
     return 0;
 }
 
-int encode_qmap(int mode, void* q, long long rowsq, long long ldq, void* tmap_out) {
+int encode_tmap_2d(void* base, int dtype, int esize, long long rows, long long cols, int box_cols, int box_rows,
+                   bool swizzle128, void* tmap_out) {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
         cudaDriverEntryPointQueryResult qr;
@@ -118,38 +120,20 @@ int encode_qmap(int mode, void* q, long long rowsq, long long ldq, void* tmap_ou
         if (qr != cudaDriverEntryPointSuccess || !fn) return fail(GBC_ECUDA, "cuTensorMapEncodeTiled unavailable");
         encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
     }
-    CUtensorMap* tm = static_cast<CUtensorMap*>(tmap_out);
-    const cuuint64_t dims[2] = {(cuuint64_t)ldq, (cuuint64_t)rowsq};
-    const cuuint64_t strides[1] = {(cuuint64_t)ldq * 2};
-    const cuuint32_t box[2] = {TC, TR};
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)cols * (cuuint64_t)esize};
+    const cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
     const cuuint32_t estr[2] = {1, 1};
-    CUresult r = encode(tm, mode == GBC_PREC_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, q,
-                        dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+    CUresult r = encode(static_cast<CUtensorMap*>(tmap_out), (CUtensorMapDataType)dtype, 2, base, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(GBC_ECUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
     return 0;
 }
 
-template <int MODE>
-__device__ __forceinline__ void unpack8(const uint4 v, float (&f)[8]) {
-    if (MODE == GBC_PREC_BF16) {
-        const unsigned w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            f[2 * i] = __uint_as_float(w[i] << 16);
-            f[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
-        }
-    } else {
-        const unsigned w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            __half2 h;
-            memcpy(&h, &w[i], 4);
-            const float2 t = __half22float2(h);
-            f[2 * i] = t.x;
-            f[2 * i + 1] = t.y;
-        }
-    }
+int encode_qmap(int mode, void* q, long long rowsq, long long ldq, void* tmap_out) {
+    return encode_tmap_2d(q, mode == GBC_PREC_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
+                          rowsq, ldq, TC, TR, false, tmap_out);
 }
 
 // y = Q x for one 32-row tile per CTA; mantle rows go to du (FP64), fault rows to y32.
@@ -259,13 +243,8 @@ __global__ void k_prologue_mixed(RhsArgs a, const double* __restrict__ u, double
             continue;
         }
         const int i = t - N;
-        const double* s = u + L.sig;
-        const double skk = (s[i] + s[i + 3 * ne] + s[i + 5 * ne]) / 3.0;
-        const double sxx = s[i] - skk, syy = s[i + 3 * ne] - skk, szz = s[i + 5 * ne] - skk;
-        const double sxy = s[i + ne], sxz = s[i + 2 * ne], syz = s[i + 4 * ne];
-        const double tau = sqrt(sxx * sxx + syy * syy + szz * szz + 2.0 * (sxy * sxy + sxz * sxz + syz * syz));
-        const double f = viscous_factor(a, i, tau);
-        const double d[6] = {f * sxx, f * sxy, f * sxz, f * syy, f * syz, f * szz};
+        double d[6];
+        viscous_rates(a, u + L.sig, i, d);
         double* deps = du + L.eps;
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
@@ -299,51 +278,11 @@ __global__ void __launch_bounds__(256) k_fault_rows_mixed(RhsArgs a, const doubl
     }
 }
 
-// Fault rows through shared memory: one CTA per (16 along-strike patches ii0..ii0+15, depth row j).
-// The CTA stages x = v - vpl for the whole fault and the Toeplitz columns st32[:, j, l] for every
-// source row l (2 N floats); thread (ii, t) sums over source rows l ≡ t (mod 16) and all k, the 16
-// partials of a patch are added in order t = 0..15, and the patch's FP64 friction follows.
-constexpr int kFR_II = 16, kFR_L = 16;
 __global__ void __launch_bounds__(kFR_II * kFR_L) k_fault_rows_smem(RhsArgs a, const double* __restrict__ u,
                                                                  double* __restrict__ du, StateLayout L) {
     if (a.skip && *a.skip) return;
     extern __shared__ float fsm[];
-    const int nx = a.nx, nxi = a.nxi, N = a.N;
-    float* xs = fsm;           // N: x[k + nx l]
-    float* ts = fsm + N;       // nx * nxi: st32[d + nx (j + nxi l)] for this j, as ts[d + nx l]
-    __shared__ float part[kFR_L][kFR_II + 1];
-    const int nb = (nx + kFR_II - 1) / kFR_II;
-    const int j = blockIdx.x / nb, ii0 = (blockIdx.x % nb) * kFR_II;
-    for (int t = threadIdx.x; t < N; t += blockDim.x) xs[t] = (float)(u[L.v + t] - a.vpl);
-    for (int t = threadIdx.x; t < N; t += blockDim.x) {
-        const int d = t % nx, l = t / nx;
-        ts[t] = a.st32[d + (size_t)nx * (j + (size_t)nxi * l)];
-    }
-    __syncthreads();
-    const int il = threadIdx.x % kFR_II, tl = threadIdx.x / kFR_II;
-    const int ii = ii0 + il;
-    float acc = 0.f;
-    if (ii < nx)
-        for (int l = tl; l < nxi; l += kFR_L) {
-            const float* x = xs + nx * l;
-            const float* tt = ts + nx * l;
-            float a0 = 0.f, a1 = 0.f;
-            int k = 0;
-            for (; k + 1 < nx; k += 2) {
-                a0 = fmaf(tt[ii > k ? ii - k : k - ii], x[k], a0);
-                a1 = fmaf(tt[ii > k + 1 ? ii - k - 1 : k + 1 - ii], x[k + 1], a1);
-            }
-            if (k < nx) a0 = fmaf(tt[ii > k ? ii - k : k - ii], x[k], a0);
-            acc += a0 + a1;
-        }
-    part[tl][il] = acc;
-    __syncthreads();
-    if (tl == 0 && ii < nx) {
-        float s = 0.f;
-        for (int t = 0; t < kFR_L; ++t) s += part[t][il];
-        const int i = ii + nx * j;
-        fault_friction(a, u, du, L, i, (double)s + (a.ne > 0 ? (double)a.y32[i] : 0.0));
-    }
+    fault_rows_cta(a, u, du, L, (int)blockIdx.x, fsm);
 }
 
 size_t fault_rows_smem_bytes(int N, int nx, int nxi) { return sizeof(float) * ((size_t)N + (size_t)nx * nxi); }

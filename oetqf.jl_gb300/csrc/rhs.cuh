@@ -102,6 +102,23 @@ __device__ __forceinline__ double viscous_factor(const RhsArgs& a, int i, double
     }
     return f;
 }
+
+// Power-law strain rates of cell i (equation.jl:285-292): d = f(τ) σ', σ' the deviatoric part of
+// the cell's stress (xx, xy, xz, yy, yz, zz) in the (ne, 6) block s and τ its second invariant.
+__device__ __forceinline__ void viscous_rates(const RhsArgs& a, const double* __restrict__ s, int i, double (&d)[6]) {
+    const int ne = a.ne;
+    const double skk = (s[i] + s[i + 3 * ne] + s[i + 5 * ne]) / 3.0;
+    const double sxx = s[i] - skk, syy = s[i + 3 * ne] - skk, szz = s[i + 5 * ne] - skk;
+    const double sxy = s[i + ne], sxz = s[i + 2 * ne], syz = s[i + 4 * ne];
+    const double tau = sqrt(sxx * sxx + syy * syy + szz * szz + 2.0 * (sxy * sxy + sxz * sxz + syz * syz));
+    const double f = viscous_factor(a, i, tau);  // equation.jl:285 (one law) or :286-292 (composite)
+    d[0] = f * sxx;
+    d[1] = f * sxy;
+    d[2] = f * sxz;
+    d[3] = f * syy;
+    d[4] = f * syz;
+    d[5] = f * szz;
+}
 #endif
 
 // Launches the RHS for the flat state u -> du on stream s (1 kernel fault-only, 2 viscoelastic).

@@ -60,13 +60,8 @@ __global__ void k_prologue(RhsArgs a, const double* __restrict__ u, double* __re
             continue;
         }
         const int i = t - N;
-        const double* s = u + L.sig;
-        const double skk = (s[i] + s[i + 3 * ne] + s[i + 5 * ne]) / 3.0;
-        const double sxx = s[i] - skk, syy = s[i + 3 * ne] - skk, szz = s[i + 5 * ne] - skk;
-        const double sxy = s[i + ne], sxz = s[i + 2 * ne], syz = s[i + 4 * ne];
-        const double tau = sqrt(sxx * sxx + syy * syy + szz * szz + 2.0 * (sxy * sxy + sxz * sxz + syz * syz));
-        const double f = viscous_factor(a, i, tau);  // equation.jl:285 (one law) or :286-292 (composite)
-        const double d[6] = {f * sxx, f * sxy, f * sxz, f * syy, f * syz, f * szz};
+        double d[6];
+        viscous_rates(a, u + L.sig, i, d);
         double* deps = du + L.eps;
 #pragma unroll
         for (int k = 0; k < 6; ++k) {

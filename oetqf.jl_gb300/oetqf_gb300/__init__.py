@@ -17,7 +17,7 @@ __all__ = ["BEMHex8Mesh", "RectOkadaMesh", "gen_mesh", "gen_hex8_box", "gauss1_q
            "DilatancyProperty", "dϵ_dt", "dϵ_dt_composite", "stress_greens_function",
            "StrikeSlip", "DipSlip", "assemble", "solve", "ArrayPartition", "GB300Model", "ODEProblem",
            "save_property", "load_property", "save_greens_functions", "load_greens_functions", "gmsh_quadrature",
-           "get_quadrature", "wsolve"]
+           "get_quadrature", "wsolve", "Sweep"]
 # identifiers are NFKC-normalised (ϵ -> ε); keep the exported names in that form
 __all__ = [_ud.normalize("NFKC", n) for n in __all__]
 
@@ -33,4 +33,7 @@ def __getattr__(name):
     if name == "wsolve":
         from . import io
         return io.wsolve
+    if name == "Sweep":
+        from . import sweep
+        return sweep.Sweep
     raise AttributeError(name)

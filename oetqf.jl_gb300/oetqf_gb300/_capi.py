@@ -17,6 +17,7 @@ LL = ctypes.c_longlong
 GBC_STRIKE_SLIP, GBC_DIP_SLIP = 0, 1
 GBC_PREC_F64, GBC_PREC_BF16, GBC_PREC_F16, GBC_PREC_DF64 = 0, 1, 2, 3
 GBC_GF11_REAL, GBC_GF11_DFT, GBC_GF12, GBC_GF21, GBC_GF22 = 0, 1, 2, 3, 4
+GBC_SWEEP_SIMT, GBC_SWEEP_UMMA = 0, 1
 ERRORS = {-1: "EINVAL", -2: "ENODEV", -3: "ECUDA", -4: "ENOMEM", -5: "ESOLVER", -6: "ESTATE"}
 
 
@@ -91,6 +92,15 @@ def lib():
             "gbc_hex_mesh_grid": [ctypes.POINTER(HexMesh), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)],
             "gbc_ensemble_integrate": [P, PD, PD, PD, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
             "gbc_ensemble_integrate_dev": [P, P, PD, PD, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
+            "gbc_sweep_create": [P, I, ctypes.POINTER(P)],
+            "gbc_sweep_set_fault_props": [P, I, PD, PD, PD, PD, D, D, D, D],
+            "gbc_sweep_set_mantle_props": [P, I, PD, PD, PD],
+            "gbc_sweep_set_engine": [P, I],
+            "gbc_sweep_rhs": [P, PD, PD],
+            "gbc_sweep_rhs_dev": [P, P, P],
+            "gbc_sweep_integrate": [P, PD, D, D, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
+            "gbc_sweep_integrate_dev": [P, P, D, D, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
+            "gbc_sweep_error_word": [P],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -112,6 +122,12 @@ def lib():
         L.gbc_ensemble_state_offset.restype = LL
         L.gbc_ensemble_stream.argtypes = [P]
         L.gbc_ensemble_stream.restype = P
+        L.gbc_sweep_destroy.argtypes = [P]
+        L.gbc_sweep_destroy.restype = None
+        L.gbc_sweep_state_len.argtypes = [P]
+        L.gbc_sweep_state_len.restype = LL
+        L.gbc_sweep_stream.argtypes = [P]
+        L.gbc_sweep_stream.restype = P
         L.gbc_model_stream.argtypes = [P]
         L.gbc_model_stream.restype = P
         L.gbc_version.restype = ctypes.c_char_p

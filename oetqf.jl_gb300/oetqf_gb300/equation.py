@@ -49,6 +49,7 @@ class GB300Model:
         self.nx, self.nξ, self.ne = nx, nξ, ne
         self.N = nx * nξ
         self.dilatancy = False
+        self.nlaws = 1
         h = ctypes.c_void_p()
         C.check(C.lib().gbc_model_create(nx, nξ, ne, ctypes.byref(h)))
         self.h = h
@@ -85,8 +86,10 @@ class GB300Model:
             gam = np.concatenate([np.asarray(q.γ, dtype=np.float64) for q in p.piter])
             nn = np.concatenate([np.asarray(q.n, dtype=np.float64) for q in p.piter])
             C.check(C.lib().gbc_model_set_mantle_props_composite(self.h, len(p.piter), k(gam), k(nn), k(p.dϵ0)))
+            self.nlaws = len(p.piter)
             return
         C.check(C.lib().gbc_model_set_mantle_props(self.h, k(p.γ), k(p.n), k(p.dϵ0)))
+        self.nlaws = 1
 
     def set_dilatancy(self, d):
         k = C.Keep()
