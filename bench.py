@@ -675,8 +675,8 @@ def main():
     ap.add_argument("--profile-rhs", type=int, default=0, help="run N right-hand sides only (for ncu captures)")
     ap.add_argument("--years", type=float, default=0.0, help="override the horizon (profiling runs only)")
     ap.add_argument("--profile-precision", default="f64", choices=["f64", "bf16", "f16", "df64"])
-    ap.add_argument("--variants", type=int, default=8, help="property variants of the sweep workload")
-    ap.add_argument("--engine", default="simt", choices=["simt", "umma"], help="product engine of the sweep workload")
+    ap.add_argument("--variants", type=int, default=32, help="property variants of the sweep workload")
+    ap.add_argument("--engine", default="umma", choices=["simt", "umma"], help="product engine of the sweep workload")
     ap.add_argument("--storage", default="f64", choices=["f64", "df64"],
                     help="mantle Green's functions of the fault-mantle workloads: FP64, or FP32 pairs (FP64-accurate)")
     args = ap.parse_args()

@@ -252,9 +252,8 @@ void* gbc_ensemble_stream(gbc_ensemble* e);
 
 typedef struct gbc_sweep gbc_sweep;
 
-#define GBC_SWEEP_SIMT 0  /* product on the FP32 pipe, each variant's sums in the single model's order
-                             (the default) */
-#define GBC_SWEEP_UMMA 1  /* product on the tensor cores (tcgen05, BF16 x BF16 -> FP32) */
+#define GBC_SWEEP_SIMT 0  /* product on the FP32 pipe, each variant's sums in the single model's order */
+#define GBC_SWEEP_UMMA 1  /* product on the tensor cores (tcgen05, BF16 x BF16 -> FP32), the default */
 
 /* nvariants (1..64) copies of a viscoelastic model's ODE (equation.jl:185-205) that share the base
  * model's Green's functions and differ in properties and state -- the reference's way of rerunning
@@ -272,7 +271,7 @@ int gbc_sweep_set_fault_props(gbc_sweep* s, int k, const double* a, const double
                               const double* sigma, double eta, double vpl, double f0, double v0);
 int gbc_sweep_set_mantle_props(gbc_sweep* s, int k, const double* gamma, const double* n,
                                const double* deps0);
-/* GBC_SWEEP_SIMT (default) or GBC_SWEEP_UMMA. */
+/* GBC_SWEEP_UMMA (default) or GBC_SWEEP_SIMT. */
 int gbc_sweep_set_engine(gbc_sweep* s, int engine);
 /* State length of one variant; states are variant-major (variant k at k * gbc_sweep_state_len). */
 long long gbc_sweep_state_len(const gbc_sweep* s);

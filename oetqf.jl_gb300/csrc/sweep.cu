@@ -576,7 +576,7 @@ using namespace gbc;
 
 struct gbc_sweep {
     gbc_model* base = nullptr;
-    int K = 0, Kp = 0, engine = GBC_SWEEP_SIMT, nlaws = 1;
+    int K = 0, Kp = 0, engine = GBC_SWEEP_UMMA, nlaws = 1;
     int N = 0, ne = 0, nx = 0, nxi = 0, npad = 0;
     long long n = 0, ldq = 0, rowsq = 0, Mpad = 0;
     cudaStream_t stream = nullptr;

@@ -20,7 +20,7 @@ class Sweep:
     functions and properties set). Each variant starts with the base's properties; ``base`` must
     outlive the sweep and keep its Green's functions."""
 
-    def __init__(self, base: GB300Model, nvariants: int, engine: str = "simt"):
+    def __init__(self, base: GB300Model, nvariants: int, engine: str = "umma"):
         h = ctypes.c_void_p()
         C.check(C.lib().gbc_sweep_create(base.h, int(nvariants), ctypes.byref(h)))
         self.h = h
