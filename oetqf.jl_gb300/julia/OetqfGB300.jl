@@ -160,4 +160,57 @@ function assemble_gb300(gf₁₁::AbstractArray, gf₁₂::AbstractMatrix, gf₂
     return ODEProblem{true}(gpu_ode, u0, tspan, m)
 end
 
+"""
+Many property sets on one assembled geometry (the example's rerun of saved Green's functions with
+other properties, examples/otf-with-mantle.jl:44-56, 140-162) integrated together: the variants share
+`base`'s block-scaled BF16 Green's functions (`gbc_model_set_precision(base, 1)` first) and every
+right-hand side is one tensor-core product over all variants' states.
+"""
+# gbc_solver_stats as an isbits struct, for arrays of them
+struct GbcStatsC
+    naccept::Clonglong; nreject::Clonglong; nrhs::Clonglong
+    t::Cdouble; dt::Cdouble
+    status::Cint
+end
+
+mutable struct GB300Sweep
+    h::Ptr{Cvoid}
+    base::GB300Model
+    nvariants::Int
+end
+
+function GB300Sweep(base::GB300Model, nvariants::Integer)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:gbc_sweep_create, libgbc), Cint, (Ptr{Cvoid}, Cint, Ref{Ptr{Cvoid}}), base.h, nvariants, h))
+    s = GB300Sweep(h[], base, nvariants)
+    finalizer(x -> ccall((:gbc_sweep_destroy, libgbc), Cvoid, (Ptr{Cvoid},), x.h), s)
+    return s
+end
+
+function set_props!(s::GB300Sweep, k::Integer, p::RateStateQuasiDynamicProperty)
+    check(ccall((:gbc_sweep_set_fault_props, libgbc), Cint,
+                (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Cdouble, Cdouble, Cdouble, Cdouble),
+                s.h, k - 1, p.a, p.b, p.L, p.σ, p.η, p.vpl, p.f₀, p.v₀))
+end
+
+function set_props!(s::GB300Sweep, k::Integer, p::PowerLawViscosityProperty)
+    check(ccall((:gbc_sweep_set_mantle_props, libgbc), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
+                s.h, k - 1, Vector{Float64}(p.γ), Vector{Float64}(p.n), Vector{Float64}(p.dϵ₀)))
+end
+
+"Integrates every variant's state (columns of `U`, each the flattened ArrayPartition) from t0 to t1."
+function solve_gb300(s::GB300Sweep, U::Matrix{Float64}, t0, t1, alg; reltol=1e-6, abstol=1e-8, dt=1e-8, dtmax=Inf,
+                     dtmin=1e-14, maxiters::Integer=10^9)
+    size(U, 2) == s.nvariants || throw(DimensionMismatch("one column per variant"))
+    code = alg isa VCABM5 ? Cint(1) : alg isa Tsit5 ? Cint(0) : throw(ArgumentError("VCABM5() or Tsit5()"))
+    o = GbcSolverOpts(reltol, abstol, dt, isfinite(dtmax) ? dtmax : 1e300, dtmin, maxiters, code)
+    st = Vector{GbcStatsC}(undef, s.nvariants)  # a C array of gbc_solver_stats
+    out = copy(U)
+    rc = ccall((:gbc_sweep_integrate, libgbc), Cint,
+               (Ptr{Cvoid}, Ptr{Cdouble}, Cdouble, Cdouble, Ref{GbcSolverOpts}, Ptr{GbcStatsC}),
+               s.h, out, t0, t1, o, st)
+    rc == 0 || rc == -5 || check(rc)
+    return out, st
+end
+
 end # module
