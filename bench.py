@@ -473,6 +473,8 @@ def run_sweep(args):
         props.append((pf, pa))
         u0s.append(u)
     sw = Sweep(m, K, engine=args.engine)
+    if args.fault_product:
+        sw.set_fault_product(True)
     for k, (pf, pa) in enumerate(props):
         sw.set_fault_props(k, pf)
         sw.set_mantle_props(k, pa)
@@ -514,18 +516,22 @@ def run_sweep(args):
     v_sw, v_1 = U[0, :N].cpu().numpy(), u[:N].cpu().numpy()
     err = float(np.abs(v_sw - v_1).max() / np.abs(v_1).max())
     matrix_bytes = (E * (N + E) + N * E) * 2
+    if args.fault_product:  # the three BF16 planes of the dense fault-fault block
+        matrix_bytes += 6 * ((N + 127) // 128 * 128) ** 2
     reads = 1 if args.engine == "umma" else (K + 7) // 8
     peak = _peak()
     ach = matrix_bytes * reads / (rhs_ms / 1e3) / 1e9
     line = _base_line(K * years / (ms / 1e3), args, 1,
                       {"workload": f"sweep-4096x8000-bf16-K{K}", "variants": K, "engine": args.engine,
+                       "fault_rows": "tensor-core product (hi/mid/lo BF16 planes)" if args.fault_product else "FP32 Toeplitz per variant",
                        "fault_patches": N, "mantle_cells": cm.ne, "window_yr": years, "solver": args.alg,
                        "rk_steps_per_variant": [int(x) for x in steps],
                        "variants_differ_in": "normal stress (+5%/variant), state distance L (+10%), mantle viscosity (+25%)",
                        "storage": "BF16 with FP32 scale per 128x128 block shared by all variants; FP32 Toeplitz; FP64 friction, theta state",
                        "l2": "inputs larger than L2"}, ms / args.steps, "bf16")
     line["roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                        "traffic": None, "kernel": f"k_sw_gemm_{args.engine} + k_sw_prologue + k_sw_fault_rows (one RHS of all variants)",
+                        "traffic": None, "kernel": f"k_sw_gemm_{args.engine} + k_sw_prologue + "
+                        f"{'k_sw_friction' if args.fault_product else 'k_sw_fault_rows'} (one RHS of all variants)",
                         "rhs_ms": rhs_ms, "bytes_per_launch": matrix_bytes * reads}
     line["single_model"] = {"value": years / (ms1 / 1e3), "unit": "sim-yr/s"}
     line["speedup_vs_single_model"] = line["value"] / line["single_model"]["value"]
@@ -677,6 +683,7 @@ def main():
     ap.add_argument("--profile-precision", default="f64", choices=["f64", "bf16", "f16", "df64"])
     ap.add_argument("--variants", type=int, default=32, help="property variants of the sweep workload")
     ap.add_argument("--engine", default="umma", choices=["simt", "umma"], help="product engine of the sweep workload")
+    ap.add_argument("--fault-product", action="store_true", help="sweep workload: fault-fault rows on the tensor cores too")
     ap.add_argument("--storage", default="f64", choices=["f64", "df64"],
                     help="mantle Green's functions of the fault-mantle workloads: FP64, or FP32 pairs (FP64-accurate)")
     args = ap.parse_args()

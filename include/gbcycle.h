@@ -273,6 +273,11 @@ int gbc_sweep_set_mantle_props(gbc_sweep* s, int k, const double* gamma, const d
                                const double* deps0);
 /* GBC_SWEEP_UMMA (default) or GBC_SWEEP_SIMT. */
 int gbc_sweep_set_engine(gbc_sweep* s, int engine);
+/* Fault rows on the tensor cores too (GBC_SWEEP_UMMA only; default off): the dense fault-fault
+ * block is built once as three BF16 planes hi + mid + lo (exact for the FP32 Toeplitz entries,
+ * 6 N^2 bytes with N rounded up to 128) and applied to all variants in the tensor-core product,
+ * leaving only the FP64 friction per variant. Off: the per-variant FP32 Toeplitz rows. */
+int gbc_sweep_set_fault_product(gbc_sweep* s, int on);
 /* State length of one variant; states are variant-major (variant k at k * gbc_sweep_state_len). */
 long long gbc_sweep_state_len(const gbc_sweep* s);
 /* ode(du, u, p, t) for every variant: u, du hold nvariants flat states (host, or device for _dev,

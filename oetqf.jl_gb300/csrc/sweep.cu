@@ -241,12 +241,24 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, unsigned parity, vo
     return false;
 }
 
+// One product launch: the 128-row tiles of a BF16 matrix (tmA) times the split state columns.
+// Mantle segment: the base model's unified rows, an FP32 scale per 128 x 128 block, results to dσ
+// and y32 (sw_store). Fault segment: the hi, mid and lo BF16 planes of the dense fault-fault block
+// (no scale), results to y[k * ldy + row].
+struct UmmaSeg {
+    long long ntiles;    // 128-row tiles
+    int nkb;             // 128-column k-blocks per tile
+    const float* scale;  // (ntiles x nkb) block scales, or nullptr
+    float* y;            // fault segment output (nullptr: mantle stores)
+    long long ldy;
+};
+
 // Warp 0 lane 0: TMA producer. Warp 1 lane 0: MMA issuer. Warps 2-5: epilogue, warp w draining
 // TMEM lanes 32 (w % 4) .. +31 (= tile rows). Persistent over 128-row tiles t = blockIdx.x + i grid.
 template <int KP>
 __global__ void __launch_bounds__(192, 1) k_sw_gemm_umma(const __grid_constant__ CUtensorMap tmA,
                                                          const __grid_constant__ CUtensorMap tmB, SweepArgs s,
-                                                         double* __restrict__ DU) {
+                                                         UmmaSeg g, double* __restrict__ DU) {
     using C = UmmaCfg<KP>;
     if (s.ndone && *s.ndone >= s.K) return;
     extern __shared__ unsigned char sm_raw[];
@@ -278,8 +290,8 @@ __global__ void __launch_bounds__(192, 1) k_sw_gemm_umma(const __grid_constant__
     __syncthreads();
     umma::fence_after();
     const uint32_t tmem = *tslot;
-    const long long ntiles = s.rowsq / 128;
-    const int nkb = (int)(s.ldq / 128);
+    const long long ntiles = g.ntiles;
+    const int nkb = g.nkb;
 
     if (warp == 0 && lane == 0) {  // ---- producer
         long long it = 0;
@@ -352,7 +364,7 @@ __global__ void __launch_bounds__(192, 1) k_sw_gemm_umma(const __grid_constant__
                 const unsigned bph = (unsigned)((it >> 1) & 1);
                 if (!wait_or_abort(&tfull[b], bph, abort_flag)) { ok = false; break; }
                 umma::fence_after();
-                const float sc = __ldg(s.qscale + t * ncb + cb);
+                const float sc = g.scale ? __ldg(g.scale + t * ncb + cb) : 1.0f;
                 const uint32_t tb = tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(b * C::N);
 #pragma unroll
                 for (int ch = 0; ch < KP / 16; ++ch) {
@@ -370,9 +382,15 @@ __global__ void __launch_bounds__(192, 1) k_sw_gemm_umma(const __grid_constant__
             }
             if (!ok) break;
             const long long row = t * 128 + 32 * quad + lane;
+            if (g.y) {
 #pragma unroll
-            for (int k = 0; k < KP; ++k)
-                if (k < s.K) sw_store(s, L, DU, k, row, acc[k]);
+                for (int k = 0; k < KP; ++k)
+                    if (k < s.K) g.y[(size_t)k * g.ldy + row] = acc[k];
+            } else {
+#pragma unroll
+                for (int k = 0; k < KP; ++k)
+                    if (k < s.K) sw_store(s, L, DU, k, row, acc[k]);
+            }
         }
         if (!ok) {
             *abort_flag = 1;
@@ -395,6 +413,41 @@ __global__ void __launch_bounds__(kFR_II * kFR_L) k_sw_fault_rows(SweepArgs s, c
     extern __shared__ float fsm[];
     const RhsArgs a = variant_view(s, k);
     fault_rows_cta(a, U + (size_t)k * s.n, DU + (size_t)k * s.n, s.lay, (int)blockIdx.x, fsm);
+}
+
+// ---- fault rows on the tensor cores ----------------------------------------------------------
+// The dense fault-fault block G11[i][k] = st32[|ii - kk| + nx (j + nxi l)] (i = ii + nx j, k = kk + nx l)
+// as three BF16 planes hi + mid + lo whose sum is the FP32 entry exactly; planes are (Nf x Nf),
+// Nf = N rounded up to 128, stacked as rows [p Nf, (p + 1) Nf), zero outside the N x N block.
+__global__ void k_sw_fault_planes(int nx, int nxi, int N, long long Nf, const float* __restrict__ st32,
+                                  uint16_t* __restrict__ qf) {
+    const long long total = Nf * Nf;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long i = e / Nf, k = e % Nf;
+        float g = 0.f;
+        if (i < N && k < N) {
+            const int ii = (int)(i % nx), j = (int)(i / nx), kk = (int)(k % nx), l = (int)(k / nx);
+            g = st32[(ii > kk ? ii - kk : kk - ii) + (size_t)nx * (j + (size_t)nxi * l)];
+        }
+        uint16_t h, m, lo;
+        bf16_split3(g, h, m, lo);
+        qf[e] = h;
+        qf[total + e] = m;
+        qf[2 * total + e] = lo;
+    }
+}
+
+// per variant (blockIdx.y): dτ = (G11 x from the three planes) + (G21 part), then the FP64 friction
+__global__ void k_sw_friction(SweepArgs s, const float* __restrict__ yf, long long Nf, const double* __restrict__ U,
+                              double* __restrict__ DU) {
+    const int k = blockIdx.y;
+    if (sw_skip(s, k)) return;
+    const RhsArgs a = variant_view(s, k);
+    const float* y = yf + (size_t)k * 3 * Nf;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.N; i += gridDim.x * blockDim.x) {
+        const float ff = (y[i] + y[Nf + i]) + y[2 * Nf + i];
+        fault_friction(a, U + (size_t)k * s.n, DU + (size_t)k * s.n, s.lay, i, (double)ff + (double)a.y32[i]);
+    }
 }
 
 // ---- integration kernels: blockIdx.y (or the thread, for the one-block kernels) = variant --------
@@ -584,6 +637,11 @@ struct gbc_sweep {
     RawBuf x32, xb, y32, err, ndone;
     alignas(128) unsigned char tmA[128];
     alignas(128) unsigned char tmB[128];
+    // fault rows on the tensor cores (optional): the hi/mid/lo planes of the dense fault-fault block
+    int fault_tc = 0;
+    long long Nf = 0;
+    RawBuf qf, yf;
+    alignas(128) unsigned char tmF[128];
     // integration
     DevBuf U, DU, k[7], y, un, phi[kAbmMax + 1], partial;
     RawBuf ctrl;
@@ -623,16 +681,24 @@ struct gbc_sweep {
 namespace gbc {
 
 template <int KP>
-static int launch_umma(const gbc_sweep* w, const SweepArgs& s, double* DU, cudaStream_t st) {
+static int launch_umma(const unsigned char* tmap_a, const gbc_sweep* w, const SweepArgs& s, const UmmaSeg& g,
+                       double* DU, cudaStream_t st) {
     using C = UmmaCfg<KP>;
     if (int rc = set_smem_limit((const void*)k_sw_gemm_umma<KP>, C::SMEM)) return rc;
-    const int grid = (int)std::min<long long>(w->rowsq / 128, sm_count());
+    const int grid = (int)std::min<long long>(g.ntiles, sm_count());
     CUtensorMap ta, tb;
-    memcpy(&ta, w->tmA, sizeof(ta));
+    memcpy(&ta, tmap_a, sizeof(ta));
     memcpy(&tb, w->tmB, sizeof(tb));
-    k_sw_gemm_umma<KP><<<grid, 192, C::SMEM, st>>>(ta, tb, s, DU);
+    k_sw_gemm_umma<KP><<<grid, 192, C::SMEM, st>>>(ta, tb, s, g, DU);
     GBC_CUDA(cudaGetLastError());
     return 0;
+}
+
+static int launch_umma_kp(const unsigned char* tmap_a, const gbc_sweep* w, const SweepArgs& s, const UmmaSeg& g,
+                          double* DU, cudaStream_t st) {
+    return s.Kp == 16 ? launch_umma<16>(tmap_a, w, s, g, DU, st)
+         : s.Kp == 32 ? launch_umma<32>(tmap_a, w, s, g, DU, st)
+                      : launch_umma<64>(tmap_a, w, s, g, DU, st);
 }
 
 // prologue, product, fault rows: three kernels for all variants
@@ -646,9 +712,17 @@ static int sweep_rhs(const gbc_sweep* w, const SweepArgs& s, const double* U, do
     else k_sw_prologue<false><<<gp, 256, 0, st>>>(s, U, DU);
     GBC_CUDA(cudaGetLastError());
     if (umma) {
-        const int rc = s.Kp == 16 ? launch_umma<16>(w, s, DU, st) : s.Kp == 32 ? launch_umma<32>(w, s, DU, st)
-                                                                                : launch_umma<64>(w, s, DU, st);
-        if (rc) return rc;
+        const UmmaSeg gm{s.rowsq / 128, (int)(s.ldq / 128), s.qscale, nullptr, 0};
+        if (int rc = launch_umma_kp(w->tmA, w, s, gm, DU, st)) return rc;
+        if (w->fault_tc) {  // fault-fault block on the tensor cores, then friction alone
+            float* yf = static_cast<float*>(w->yf.p);
+            const UmmaSeg gf{3 * w->Nf / 128, (int)(w->Nf / 128), nullptr, yf, 3 * w->Nf};
+            if (int rc = launch_umma_kp(w->tmF, w, s, gf, DU, st)) return rc;
+            int gx = (s.N + 255) / 256;
+            k_sw_friction<<<dim3((unsigned)gx, (unsigned)s.K), 256, 0, st>>>(s, yf, w->Nf, U, DU);
+            GBC_CUDA(cudaGetLastError());
+            return 0;
+        }
     } else {
         const dim3 gg((unsigned)(s.rowsq / kSwRows), (unsigned)((s.K + kSwGroup - 1) / kSwGroup));
         k_sw_gemm_simt<<<gg, 256, 0, st>>>(s, DU);
@@ -662,7 +736,8 @@ static int sweep_rhs(const gbc_sweep* w, const SweepArgs& s, const double* U, do
     return 0;
 }
 
-constexpr int kSwRhsKernels = 3;
+// kernels one sweep_rhs launches: prologue, product(s), fault rows or friction
+static int sweep_rhs_kernels(const gbc_sweep* w) { return (w->engine == GBC_SWEEP_UMMA && w->fault_tc) ? 4 : 3; }
 
 static int sweep_tsit5_step(gbc_sweep* w, cudaStream_t st) {
     const long long n = w->n;
@@ -844,6 +919,31 @@ int gbc_sweep_set_engine(gbc_sweep* w, int engine) {
     return 0;
 }
 
+int gbc_sweep_set_fault_product(gbc_sweep* w, int on) {
+    if (!w) return fail(GBC_EINVAL, "null sweep");
+    if (!on) {
+        w->fault_tc = 0;
+        return 0;
+    }
+    if (int rc = w->check_base()) return rc;
+    w->Nf = ((long long)w->N + 127) / 128 * 128;
+    const long long planes = w->Nf * w->Nf;
+    if (int rc = w->qf.alloc(2 * 3 * (size_t)planes)) return rc;
+    if (int rc = w->yf.alloc(sizeof(float) * 3 * (size_t)w->Nf * w->K)) return rc;
+    cudaStream_t s = w->stream;
+    GBC_CUDA(cudaMemsetAsync(w->yf.p, 0, w->yf.bytes, s));
+    k_sw_fault_planes<<<sm_count() * 8, 256, 0, s>>>(w->nx, w->nxi, w->N, w->Nf,
+                                                     static_cast<const float*>(w->base->st32.p),
+                                                     static_cast<uint16_t*>(w->qf.p));
+    GBC_CUDA(cudaGetLastError());
+    count_launches(1);
+    if (int rc = encode_tmap_2d(w->qf.p, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, 3 * w->Nf, w->Nf, 64, 128, true, w->tmF))
+        return rc;
+    GBC_CUDA(cudaStreamSynchronize(s));
+    w->fault_tc = 1;
+    return 0;
+}
+
 int gbc_sweep_set_fault_props(gbc_sweep* w, int k, const double* a, const double* b, const double* L,
                               const double* sigma, double eta, double vpl, double f0, double v0) {
     if (!w || !a || !b || !L || !sigma) return fail(GBC_EINVAL, "null argument");
@@ -880,7 +980,7 @@ int gbc_sweep_rhs_dev(gbc_sweep* w, const double* u, double* du) {
     if (!w || !u || !du) return fail(GBC_EINVAL, "null argument");
     if (int rc = w->check_base()) return rc;
     if (int rc = sweep_rhs(w, w->args(nullptr, 0), u, du, w->stream)) return rc;
-    count_launches(kSwRhsKernels);
+    count_launches(sweep_rhs_kernels(w));
     return 0;
 }
 
@@ -953,8 +1053,9 @@ int gbc_sweep_integrate_dev(gbc_sweep* w, double* u_dev, double t0, double t1, c
     GBC_CUDA(cudaMemcpyAsync(w->ctrl_host, w->ctrl.p, sizeof(Ctrl) * w->K, cudaMemcpyDeviceToHost, s));
     if (u_dev != w->U.p) GBC_CUDA(cudaMemcpyAsync(u_dev, w->U.p, sizeof(double) * kn, cudaMemcpyDeviceToDevice, s));
     GBC_CUDA(cudaStreamSynchronize(s));
-    const long long per_step = (o->alg == GBC_ALG_VCABM5) ? 6 + 2LL * kSwRhsKernels : 10 + 6LL * kSwRhsKernels;
-    count_launches(kSwRhsKernels + w->graph_launches * w->steps_per_launch * per_step);
+    const long long rk = sweep_rhs_kernels(w);
+    const long long per_step = (o->alg == GBC_ALG_VCABM5) ? 6 + 2 * rk : 10 + 6 * rk;
+    count_launches(rk + w->graph_launches * w->steps_per_launch * per_step);
     int status = 0;
     for (int k = 0; k < w->K; ++k) {
         const Ctrl& c = w->ctrl_host[k];

@@ -96,6 +96,7 @@ def lib():
             "gbc_sweep_set_fault_props": [P, I, PD, PD, PD, PD, D, D, D, D],
             "gbc_sweep_set_mantle_props": [P, I, PD, PD, PD],
             "gbc_sweep_set_engine": [P, I],
+            "gbc_sweep_set_fault_product": [P, I],
             "gbc_sweep_rhs": [P, PD, PD],
             "gbc_sweep_rhs_dev": [P, P, P],
             "gbc_sweep_integrate": [P, PD, D, D, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],

@@ -48,6 +48,10 @@ class Sweep:
         C.check(C.lib().gbc_sweep_set_engine(self.h, ENGINES[engine]))
         self.engine = engine
 
+    def set_fault_product(self, on: bool):
+        """Run the fault-fault block in the tensor-core product as well (engine "umma"; default off)."""
+        C.check(C.lib().gbc_sweep_set_fault_product(self.h, int(bool(on))))
+
     def set_fault_props(self, k: int, p):
         """RateStateQuasiDynamicProperty of variant k."""
         for name in ("a", "b", "L", "σ"):
