@@ -143,22 +143,23 @@ def cpu_oracle_model(cm, gfs=None):
     import oracle as O
     gf11 = O.gf_ff(cm.mf, cm.lam, cm.mu, fourier=True)
     if not cm.ne:
-        return O, O.OracleModel(gf11, cm.pf), "exact"
+        return O, O.OracleModel(gf11, cm.pf), "exact", (gf11,)
     if gfs is not None:
-        return O, O.OracleModel(gf11, cm.pf, *gfs, cm.pa), "exact (exported from the device assembly)"
+        return O, O.OracleModel(gf11, cm.pf, *gfs, cm.pa), "exact (exported from the device assembly)", (gf11, *gfs)
     g12 = O.gf_fm(cm.mf, cm.ma, cm.lam, cm.mu)
     vol = np.tile(cm.ma.Δx * cm.ma.Δy * cm.ma.Δz, 6) * np.repeat([1.0, 2, 2, 1, 2, 1], cm.ne)
     area = cm.mf.Δx * cm.mf.Δξ
     g21 = np.ascontiguousarray((g12 * vol[:, None]).T / area)
     g22 = np.diag(np.full(6 * cm.ne, -cm.mu))
-    return O, O.OracleModel(gf11, cm.pf, g12, g21, g22, cm.pa), "stand-in mantle values (timing is value-independent)"
+    return (O, O.OracleModel(gf11, cm.pf, g12, g21, g22, cm.pa), "stand-in mantle values (timing is value-independent)",
+            (gf11, g12, g21, g22))
 
 
 def cpu_oracle_sample(cm, name, alg, gfs=None, budget_s=20.0, nrhs_horizon=None):
     """Times the oracle (all host threads) over a bounded number of steps of the full-size workload
     with the same integrator and scales by the RHS evaluations that integrator takes for the whole
     horizon (from the table, or as counted on the device in the same run)."""
-    O, om, how = cpu_oracle_model(cm, gfs)
+    O, om, how, pack = cpu_oracle_model(cm, gfs)
     t0 = time.perf_counter()
     om.ode(cm.u0)
     t_rhs = time.perf_counter() - t0
@@ -171,10 +172,35 @@ def cpu_oracle_sample(cm, name, alg, gfs=None, budget_s=20.0, nrhs_horizon=None)
     per_rhs = wall / max(st.nrhs, 1)
     total_rhs = RHS_FOR_HORIZON.get((name, alg), nrhs_horizon)
     total = per_rhs * total_rhs
-    return {"value": (cm.horizon / YEAR) / total, "unit": "sim-yr/s", "cores": O.num_threads(), "kind": "port",
-            "sample": f"{st.naccept + st.nreject} {alg} steps ({st.nrhs} RHS) of the full-size workload on the "
-                      f"C/OpenMP FP64 oracle ({per_rhs * 1e3:.2f} ms/RHS, Green's functions: {how}), scaled to the "
-                      f"{total_rhs} RHS evaluations the same integrator takes for {cm.horizon / YEAR:.0f} yr"}
+    out = {"value": (cm.horizon / YEAR) / total, "unit": "sim-yr/s", "cores": O.num_threads(), "kind": "port",
+           "sample": f"{st.naccept + st.nreject} {alg} steps ({st.nrhs} RHS) of the full-size workload on the "
+                     f"C/OpenMP FP64 oracle ({per_rhs * 1e3:.2f} ms/RHS, Green's functions: {how}), scaled to the "
+                     f"{total_rhs} RHS evaluations the same integrator takes for {cm.horizon / YEAR:.0f} yr"}
+    return out, (pack, how, total_rhs)
+
+
+def cpu_twin_sample(cm, pack, how, total_rhs, budget_s=8.0):
+    """The numpy/scipy twin of the reference's RHS (FFT convolution, BLAS GEMVs, vectorised friction;
+    oracle/numpy_twin.py) timed over a bounded number of right-hand sides on all host threads and
+    scaled to the RHS evaluations of the whole horizon (integrator overhead not included)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from numpy_twin import NumpyTwin
+    tw = NumpyTwin(pack[0], cm.pf, *pack[1:], cm.pa) if cm.ne else NumpyTwin(pack[0], cm.pf)
+    tw.ode(cm.u0)
+    t0 = time.perf_counter()
+    tw.ode(cm.u0)
+    t1 = time.perf_counter() - t0
+    n = int(min(500, max(3, budget_s / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(n):
+        tw.ode(cm.u0)
+    per_rhs = (time.perf_counter() - t0) / n
+    return {"value": (cm.horizon / YEAR) / (per_rhs * total_rhs), "unit": "sim-yr/s", "cores": os.cpu_count(),
+            "kind": "port",
+            "sample": f"{n} right-hand sides of the full-size workload on the numpy/scipy twin of the reference's "
+                      f"library structure (scipy.fft convolution, numpy BLAS GEMVs; {per_rhs * 1e3:.2f} ms/RHS, Green's "
+                      f"functions: {how}), scaled to the {total_rhs} RHS evaluations of the horizon; integrator "
+                      f"overhead not included"}
 
 
 def run_reference(args):
@@ -184,7 +210,7 @@ def run_reference(args):
     cm = workload(args.workload)
     vals = []
     for _ in range(args.steps):
-        vals.append(cpu_oracle_sample(cm, args.workload, args.alg, budget_s=args.cpu_budget / max(args.steps, 1)))
+        vals.append(cpu_oracle_sample(cm, args.workload, args.alg, budget_s=args.cpu_budget / max(args.steps, 1))[0])
     v = statistics.median([x["value"] for x in vals])
     base = vals[0]
     base["value"] = v
@@ -356,8 +382,9 @@ def run_gpu(args):
         line["max_slip_rate_rel_err_vs_f64_1yr"] = err_vs_f64
     if not args.no_cpu:
         gfs = tuple(m.export_gf(w) for w in (C.GBC_GF12, C.GBC_GF21, C.GBC_GF22)) if cm.ne else None
-        line["cpu_baseline"] = cpu_oracle_sample(cm, args.workload, args.alg, gfs=gfs, budget_s=args.cpu_budget,
-                                                 nrhs_horizon=nrhs)
+        line["cpu_baseline"], (pack, how, total_rhs) = cpu_oracle_sample(cm, args.workload, args.alg, gfs=gfs,
+                                                                         budget_s=args.cpu_budget, nrhs_horizon=nrhs)
+        line["cpu_baseline_twin"] = cpu_twin_sample(cm, pack, how, total_rhs)
     print(json.dumps(line), flush=True)
 
 
