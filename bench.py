@@ -395,6 +395,11 @@ def run_gpu(args):
         line["cpu_baseline"], (pack, how, total_rhs) = cpu_oracle_sample(cm, args.workload, args.alg, gfs=gfs,
                                                                          budget_s=args.cpu_budget, nrhs_horizon=nrhs)
         line["cpu_baseline_twin"] = cpu_twin_sample(cm, pack, how, total_rhs)
+    if not args.no_sweep and ws == 1:
+        try:  # the tensor-core form: property variants sharing one geometry's Green's functions
+            line["sweep"] = sweep_summary(args)
+        except Exception as exc:
+            line["sweep"] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
     print(json.dumps(line), flush=True)
 
 
@@ -482,17 +487,17 @@ def run_mixed_large(args):
     print(json.dumps(line), flush=True)
 
 
-def run_sweep(args):
+def sweep_measure(K, engine, years, steps, alg, warmup=3, fault_product=False):
     """Property variants of the 4096-patch + 8000-cell model sharing its block-scaled BF16 Green's
-    functions (gbc_sweep): aggregate sim-yr/s over a window against the single-model BF16 path."""
+    functions (gbc_sweep) over a window, and the single-model BF16 path on variant 0 over the same
+    window in the same run. Returns the measurements (times from CUDA events on the sweep's and the
+    model's streams)."""
     import torch
     from oetqf_gb300 import _capi as C
     from oetqf_gb300.equation import GB300Model
     from oetqf_gb300.property import PowerLawViscosityProperty, RateStateQuasiDynamicProperty
     from oetqf_gb300.sweep import Sweep
     cm = large_fault_with_mantle()
-    years = args.years or 20.0
-    K = args.variants
     m = GB300Model(cm.mf.nx, cm.mf.nξ, cm.ne)
     m.assemble_gf(cm.mf, cm.ma, cm.lam, cm.mu)
     m.set_fault_props(cm.pf)
@@ -509,8 +514,8 @@ def run_sweep(args):
         u[N:2 * N] *= l_k
         props.append((pf, pa))
         u0s.append(u)
-    sw = Sweep(m, K, engine=args.engine)
-    if args.fault_product:
+    sw = Sweep(m, K, engine=engine)
+    if fault_product:
         sw.set_fault_product(True)
     for k, (pf, pa) in enumerate(props):
         sw.set_fault_props(k, pf)
@@ -518,7 +523,7 @@ def run_sweep(args):
     stream = torch.cuda.ExternalStream(sw.stream)
     U = torch.tensor(np.stack(u0s), device="cuda")
     DU = torch.zeros_like(U)
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(max(warmup, 3)):
         sw.rhs_dev(U.data_ptr(), DU.data_ptr())
     r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     r0.record(stream)
@@ -527,52 +532,78 @@ def run_sweep(args):
     r1.record(stream)
     r1.synchronize()
     rhs_ms = r0.elapsed_time(r1) / 20
-    edges = np.linspace(0.0, years * YEAR, args.steps + 1)
+    edges = np.linspace(0.0, years * YEAR, steps + 1)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    steps = np.zeros(K, dtype=np.int64)
-    for i in range(args.steps):
-        st = sw.integrate_dev(U.data_ptr(), float(edges[i]), float(edges[i + 1]), alg=args.alg, **SOLVER)
-        steps += np.array([s.naccept + s.nreject for s in st])
+    rk = np.zeros(K, dtype=np.int64)
+    for i in range(steps):
+        st = sw.integrate_dev(U.data_ptr(), float(edges[i]), float(edges[i + 1]), alg=alg, **SOLVER)
+        rk += np.array([s.naccept + s.nreject for s in st])
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
-    assert sw.error_word() == 0
-    # the single-model BF16 path on variant 0 (the base's own properties) over the same window
+    if sw.error_word() != 0:
+        raise RuntimeError("sweep pipeline wait timed out")
     stream1 = torch.cuda.ExternalStream(m.stream)
     u = torch.tensor(u0s[0], device="cuda")
     torch.cuda.synchronize()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream1)
-    for i in range(args.steps):
-        m.integrate_dev(u.data_ptr(), float(edges[i]), float(edges[i + 1]), alg=args.alg, **SOLVER)
+    for i in range(steps):
+        m.integrate_dev(u.data_ptr(), float(edges[i]), float(edges[i + 1]), alg=alg, **SOLVER)
     f1.record(stream1)
     f1.synchronize()
     ms1 = f0.elapsed_time(f1)
     v_sw, v_1 = U[0, :N].cpu().numpy(), u[:N].cpu().numpy()
-    err = float(np.abs(v_sw - v_1).max() / np.abs(v_1).max())
     matrix_bytes = (E * (N + E) + N * E) * 2
-    if args.fault_product:  # the three BF16 planes of the dense fault-fault block
+    if fault_product:  # the three BF16 planes of the dense fault-fault block
         matrix_bytes += 6 * ((N + 127) // 128 * 128) ** 2
-    reads = 1 if args.engine == "umma" else (K + 7) // 8
+    reads = 1 if engine == "umma" else (K + 7) // 8
+    sw.close()
+    m.close()
+    return {"value": K * years / (ms / 1e3), "ms": ms, "rhs_ms": rhs_ms, "single_value": years / (ms1 / 1e3),
+            "rk_steps": [int(x) for x in rk], "err": float(np.abs(v_sw - v_1).max() / np.abs(v_1).max()),
+            "bytes": matrix_bytes * reads, "N": N, "ne": cm.ne}
+
+
+def sweep_summary(args):
+    """The shared-geometry sweep on the tensor cores, 32 variants of the 4096 + 8000 model over one
+    20-year window, for the default bench line."""
+    r = sweep_measure(32, "umma", 20.0, 1, args.alg)
     peak = _peak()
-    ach = matrix_bytes * reads / (rhs_ms / 1e3) / 1e9
-    line = _base_line(K * years / (ms / 1e3), args, 1,
+    ach = r["bytes"] / (r["rhs_ms"] / 1e3) / 1e9
+    return {"workload": "sweep-4096x8000-bf16-K32", "variants": 32, "engine": "tcgen05", "window_yr": 20.0,
+            "value": r["value"], "unit": "sim-yr/s (all variants)", "single_model_bf16": r["single_value"],
+            "speedup_vs_single_model": r["value"] / r["single_value"],
+            "rhs_ms_all_variants": r["rhs_ms"], "rhs_roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak},
+            "rk_steps_per_variant_min_max": [min(r["rk_steps"]), max(r["rk_steps"])],
+            "variant0_max_slip_rate_rel_diff_vs_single_model": r["err"]}
+
+
+def run_sweep(args):
+    """Property variants of the 4096-patch + 8000-cell model sharing its block-scaled BF16 Green's
+    functions (gbc_sweep): aggregate sim-yr/s over a window against the single-model BF16 path."""
+    years = args.years or 20.0
+    K = args.variants
+    r = sweep_measure(K, args.engine, years, args.steps, args.alg, args.warmup, args.fault_product)
+    peak = _peak()
+    ach = r["bytes"] / (r["rhs_ms"] / 1e3) / 1e9
+    line = _base_line(r["value"], args, 1,
                       {"workload": f"sweep-4096x8000-bf16-K{K}", "variants": K, "engine": args.engine,
                        "fault_rows": "tensor-core product (hi/mid/lo BF16 planes)" if args.fault_product else "FP32 Toeplitz per variant",
-                       "fault_patches": N, "mantle_cells": cm.ne, "window_yr": years, "solver": args.alg,
-                       "rk_steps_per_variant": [int(x) for x in steps],
+                       "fault_patches": r["N"], "mantle_cells": r["ne"], "window_yr": years, "solver": args.alg,
+                       "rk_steps_per_variant": r["rk_steps"],
                        "variants_differ_in": "normal stress (+5%/variant), state distance L (+10%), mantle viscosity (+25%)",
                        "storage": "BF16 with FP32 scale per 128x128 block shared by all variants; FP32 Toeplitz; FP64 friction, theta state",
-                       "l2": "inputs larger than L2"}, ms / args.steps, "bf16")
+                       "l2": "inputs larger than L2"}, r["ms"] / args.steps, "bf16")
     line["roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                         "traffic": None, "kernel": f"k_sw_gemm_{args.engine} + k_sw_prologue + "
                         f"{'k_sw_friction' if args.fault_product else 'k_sw_fault_rows'} (one RHS of all variants)",
-                        "rhs_ms": rhs_ms, "bytes_per_launch": matrix_bytes * reads}
-    line["single_model"] = {"value": years / (ms1 / 1e3), "unit": "sim-yr/s"}
-    line["speedup_vs_single_model"] = line["value"] / line["single_model"]["value"]
-    line["variant0_max_slip_rate_rel_diff_vs_single_model"] = err
+                        "rhs_ms": r["rhs_ms"], "bytes_per_launch": r["bytes"]}
+    line["single_model"] = {"value": r["single_value"], "unit": "sim-yr/s"}
+    line["speedup_vs_single_model"] = line["value"] / r["single_value"]
+    line["variant0_max_slip_rate_rel_diff_vs_single_model"] = r["err"]
     print(json.dumps(line), flush=True)
 
 
@@ -721,6 +752,7 @@ def main():
     ap.add_argument("--variants", type=int, default=32, help="property variants of the sweep workload")
     ap.add_argument("--engine", default="umma", choices=["simt", "umma"], help="product engine of the sweep workload")
     ap.add_argument("--fault-product", action="store_true", help="sweep workload: fault-fault rows on the tensor cores too")
+    ap.add_argument("--no-sweep", action="store_true", help="default line: skip the shared-geometry sweep sub-measurement")
     ap.add_argument("--storage", default="f64", choices=["f64", "df64"],
                     help="mantle Green's functions of the fault-mantle workloads: FP64, or FP32 pairs (FP64-accurate)")
     args = ap.parse_args()
