@@ -487,17 +487,21 @@ def run_mixed_large(args):
     print(json.dumps(line), flush=True)
 
 
-def sweep_measure(K, engine, years, steps, alg, warmup=3, fault_product=False):
-    """Property variants of the 4096-patch + 8000-cell model sharing its block-scaled BF16 Green's
-    functions (gbc_sweep) over a window, and the single-model BF16 path on variant 0 over the same
-    window in the same run. Returns the measurements (times from CUDA events on the sweep's and the
-    model's streams)."""
+SWEEP_GEOMETRY = {"sweep-4096x8000": large_fault_with_mantle, "sweep-1000x2500": strike_slip_with_mantle}
+
+
+def sweep_measure(K, engine, years, steps, alg, warmup=3, fault_product=False, geometry="sweep-4096x8000",
+                  profile_rhs=0):
+    """Property variants of a viscoelastic model sharing its block-scaled BF16 Green's functions
+    (gbc_sweep) over a window, and the single-model BF16 path on variant 0 over the same window in
+    the same run. Returns the measurements (times from CUDA events on the sweep's and the model's
+    streams). With profile_rhs > 0 only that many right-hand sides of all variants run (for ncu)."""
     import torch
     from oetqf_gb300 import _capi as C
     from oetqf_gb300.equation import GB300Model
     from oetqf_gb300.property import PowerLawViscosityProperty, RateStateQuasiDynamicProperty
     from oetqf_gb300.sweep import Sweep
-    cm = large_fault_with_mantle()
+    cm = SWEEP_GEOMETRY[geometry]()
     m = GB300Model(cm.mf.nx, cm.mf.nξ, cm.ne)
     m.assemble_gf(cm.mf, cm.ma, cm.lam, cm.mu)
     m.set_fault_props(cm.pf)
@@ -523,6 +527,14 @@ def sweep_measure(K, engine, years, steps, alg, warmup=3, fault_product=False):
     stream = torch.cuda.ExternalStream(sw.stream)
     U = torch.tensor(np.stack(u0s), device="cuda")
     DU = torch.zeros_like(U)
+    if profile_rhs:
+        for _ in range(profile_rhs):
+            sw.rhs_dev(U.data_ptr(), DU.data_ptr())
+        torch.cuda.synchronize()
+        err = sw.error_word()
+        sw.close()
+        m.close()
+        return {"profile_rhs": profile_rhs, "error_word": err}
     for _ in range(max(warmup, 3)):
         sw.rhs_dev(U.data_ptr(), DU.data_ptr())
     r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -586,11 +598,15 @@ def run_sweep(args):
     functions (gbc_sweep): aggregate sim-yr/s over a window against the single-model BF16 path."""
     years = args.years or 20.0
     K = args.variants
-    r = sweep_measure(K, args.engine, years, args.steps, args.alg, args.warmup, args.fault_product)
+    r = sweep_measure(K, args.engine, years, args.steps, args.alg, args.warmup, args.fault_product, args.workload,
+                      args.profile_rhs)
+    if args.profile_rhs:
+        print(json.dumps(r), flush=True)
+        return
     peak = _peak()
     ach = r["bytes"] / (r["rhs_ms"] / 1e3) / 1e9
     line = _base_line(r["value"], args, 1,
-                      {"workload": f"sweep-4096x8000-bf16-K{K}", "variants": K, "engine": args.engine,
+                      {"workload": f"{args.workload}-bf16-K{K}", "variants": K, "engine": args.engine,
                        "fault_rows": "tensor-core product (hi/mid/lo BF16 planes)" if args.fault_product else "FP32 Toeplitz per variant",
                        "fault_patches": r["N"], "mantle_cells": r["ne"], "window_yr": years, "solver": args.alg,
                        "rk_steps_per_variant": r["rk_steps"],
@@ -736,7 +752,7 @@ def main():
     ap.add_argument("--impl", default="gbcycle", choices=["gbcycle", "reference"])
     ap.add_argument("--workload", default="fault-mantle-1000x2500-f64",
                     choices=WORKLOADS + ["fault-mantle-4096x8000-mixed", "ensemble-256", "serving",
-                                                       "ensemble-profile", "sweep-4096x8000"])
+                                                       "ensemble-profile", "sweep-4096x8000", "sweep-1000x2500"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "f16"])
     ap.add_argument("--alg", default=None, choices=["VCABM5", "Tsit5"],
                     help="integrator (default: VCABM5, the reference example's solver; with it the state holds θ; "
@@ -768,7 +784,7 @@ def main():
         run_ensemble_profile(args)
     elif args.workload == "serving":
         run_serving(args)
-    elif args.workload == "sweep-4096x8000":
+    elif args.workload.startswith("sweep-"):
         run_sweep(args)
     else:
         run_gpu(args)
