@@ -6,6 +6,7 @@ model's order)."""
 from __future__ import annotations
 
 import ctypes
+import time
 
 import numpy as np
 
@@ -107,6 +108,21 @@ class Sweep:
         if rc < 0 and rc != -5:
             C.check(rc)
         return list(st)
+
+    def autotune(self, u: np.ndarray, candidates=("umma", "simt"), reps: int = 5):
+        """Times `reps` right-hand sides of all variants at the states u with each engine and keeps
+        the fastest; returns (engine, {engine: seconds})."""
+        timings = {}
+        for eng in candidates:
+            self.set_engine(eng)
+            self.rhs(u)  # first call: staging buffers, kernel attributes
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                self.rhs(u)
+            timings[eng] = time.perf_counter() - t0
+        best = min(timings, key=timings.get)
+        self.set_engine(best)
+        return best, timings
 
     def error_word(self) -> int:
         return int(C.lib().gbc_sweep_error_word(self.h))
