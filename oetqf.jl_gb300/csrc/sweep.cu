@@ -526,8 +526,9 @@ __global__ void k_sw_commit(long long n, double* __restrict__ U, const double* _
     if (!ctrl[blockIdx.y].accept) return;
     const size_t off = (size_t)blockIdx.y * n;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        U[off + i] = UN[off + i];
-        K0[off + i] = K6[off + i];
+        const double un = UN[off + i], k6 = K6[off + i];  // both loads ahead of the stores
+        U[off + i] = un;
+        K0[off + i] = k6;
     }
 }
 
@@ -609,14 +610,19 @@ __global__ void k_sw_abm_commit(long long n, double* __restrict__ U, const doubl
     for (int j = 0; j < kAbmMax; ++j) beta[j] = c->beta[j];
     const size_t off = (size_t)blockIdx.y * n;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        U[off + i] = UN[off + i];
+        // every old difference is loaded before any is overwritten: the arrays are distinct, and
+        // loading first keeps the loads from queueing one by one behind the stores
+        double old[kAbmMax];
+#pragma unroll
+        for (int j = 0; j < kAbmMax; ++j) old[j] = (j < k) ? P.p[j][off + i] : 0.0;
+        const double un = UN[off + i];
         double nw = FN[off + i];
+        U[off + i] = un;
 #pragma unroll
         for (int j = 0; j < kAbmMax; ++j) {
             if (j < k) {
-                const double old = P.p[j][off + i];
                 P.p[j][off + i] = nw;
-                nw = nw - beta[j] * old;
+                nw = nw - beta[j] * old[j];
             }
         }
         P.p[k][off + i] = nw;
