@@ -590,10 +590,11 @@ __global__ void k_sw_abm_correct(long long n, const double* __restrict__ U, cons
     double ss = 0.0;
     int bad = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double ui = U[off + i];  // loaded ahead of the store to UN
         const double pk = FP[off + i] - SV[off + i];
         const double yn = YP[off + i] + h * gk * pk;
         UN[off + i] = yn;
-        const double r = ce * pk / (atol + rtol * fmax(fabs(U[off + i]), fabs(yn)));
+        const double r = ce * pk / (atol + rtol * fmax(fabs(ui), fabs(yn)));
         ss = fma(r, r, ss);
         bad |= !isfinite(yn);
     }
