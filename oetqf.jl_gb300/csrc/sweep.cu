@@ -526,9 +526,8 @@ __global__ void k_sw_commit(long long n, double* __restrict__ U, const double* _
     if (!ctrl[blockIdx.y].accept) return;
     const size_t off = (size_t)blockIdx.y * n;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const double un = UN[off + i], k6 = K6[off + i];  // both loads ahead of the stores
-        U[off + i] = un;
-        K0[off + i] = k6;
+        U[off + i] = UN[off + i];
+        K0[off + i] = K6[off + i];
     }
 }
 
@@ -590,11 +589,10 @@ __global__ void k_sw_abm_correct(long long n, const double* __restrict__ U, cons
     double ss = 0.0;
     int bad = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const double ui = U[off + i];  // loaded ahead of the store to UN
         const double pk = FP[off + i] - SV[off + i];
         const double yn = YP[off + i] + h * gk * pk;
         UN[off + i] = yn;
-        const double r = ce * pk / (atol + rtol * fmax(fabs(ui), fabs(yn)));
+        const double r = ce * pk / (atol + rtol * fmax(fabs(U[off + i]), fabs(yn)));
         ss = fma(r, r, ss);
         bad |= !isfinite(yn);
     }
@@ -611,8 +609,9 @@ __global__ void k_sw_abm_commit(long long n, double* __restrict__ U, const doubl
     for (int j = 0; j < kAbmMax; ++j) beta[j] = c->beta[j];
     const size_t off = (size_t)blockIdx.y * n;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        // every old difference is loaded before any is overwritten: the arrays are distinct, and
-        // loading first keeps the loads from queueing one by one behind the stores
+        // every old difference is loaded before any is overwritten: the arrays are distinct, but
+        // pointers held in a struct carry no no-alias promise, so loads interleaved with the stores
+        // would each wait for the store before them
         double old[kAbmMax];
 #pragma unroll
         for (int j = 0; j < kAbmMax; ++j) old[j] = (j < k) ? P.p[j][off + i] : 0.0;
