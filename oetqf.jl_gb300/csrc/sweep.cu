@@ -100,7 +100,9 @@ __device__ __forceinline__ bool sw_skip(const SweepArgs& s, int k) {
     return s.skip == 1 ? c.done != 0 : (c.done != 0 || c.skip2 != 0);
 }
 
-// x = hi + mid + lo exactly: each residual is exact in FP32 and holds at most 16, then 8 bits
+// x = hi + mid + lo exactly for 2^-102 <= |x| < 2^128 (1 - 2^-9): each residual is exact in FP32
+// and holds at most 16, then 8 significant bits (below the range the last part rounds to a BF16
+// subnormal, off by at most 2^-134; above it bf16(x) overflows)
 __device__ __forceinline__ void bf16_split3(float x, uint16_t& h, uint16_t& m, uint16_t& l) {
     const __nv_bfloat16 bh = __float2bfloat16_rn(x);
     const float r1 = __fsub_rn(x, __bfloat162float(bh));
