@@ -14,8 +14,10 @@
 //    A 128 x 128 k-block is one scale block of the matrix, so each k-block's MMAs start a fresh
 //    accumulator and the epilogue warps apply the block's FP32 scale as they drain it from TMEM
 //    (two accumulators alternate so the drain overlaps the next k-block's MMAs).
-// The fault rows (FP32 Toeplitz sum + the G21 part, FP64 friction) run per variant with the single
-// model's kernel body. Integration: each variant has its own step size, error norm and
+// UMMA is the default engine. The fault rows (FP32 Toeplitz sum + the G21 part, FP64 friction) run
+// per variant with the single model's kernel body; optionally (gbc_sweep_set_fault_product) the
+// dense fault-fault block joins the tensor-core product as a second segment of exact hi/mid/lo BF16
+// planes and only the friction stays per variant. Integration: each variant has its own step size, error norm and
 // accept/reject (the single model's Tsit5 or VCABM5 controllers); the variants go through the
 // stages together so one product serves all of them, and a variant that reached t1 stops changing.
 //
