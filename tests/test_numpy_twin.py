@@ -44,3 +44,26 @@ def test_twin_viscoelastic_matches_oracle(oracle):
     got = NumpyTwin(gfs[0], pf, *gfs[1:], pa).ode(u)
     for part in (slice(0, N), slice(N, 2 * N), slice(2 * N, 2 * N + M), slice(2 * N + M, 2 * N + 2 * M), slice(2 * N + 2 * M, None)):
         np.testing.assert_allclose(got[part], ref[part], rtol=1e-9, atol=1e-12 * np.abs(ref[part]).max())
+
+
+def test_twin_composite_viscosity_matches_oracle(oracle):
+    from numpy_twin import NumpyTwin
+
+    from oetqf_gb300 import CompositePowerLawViscosityProperty
+    mf = gen_mesh("RectOkada", 20e3, 4e3, 2e3, 1e3, 90.0)
+    ma = gen_hex8_box(-10e3, -4e3, -6e3, 20e3, 8e3, -8e3, 2, 2, 2)
+    mu = 3e10
+    gfs = [oracle.gf_ff(mf, mu, mu, fourier=True), oracle.gf_fm(mf, ma, mu, mu), oracle.gf_mf(ma, mf, mu, mu),
+           oracle.gf_mm(ma, mu, mu)]
+    rng = np.random.default_rng(13)
+    pf = _fault(mf, mu, rng)
+    pa = CompositePowerLawViscosityProperty([PowerLawViscosityProperty(np.full(ma.ne, 5e-20), np.zeros(ma.ne), np.zeros(6)),
+                                             PowerLawViscosityProperty(np.full(ma.ne, 1e-30), np.full(ma.ne, 2.0), np.zeros(6))],
+                                            np.array([0.0, 1e-15, 0, 0, 0, 0]))
+    N, M = mf.nx * mf.nξ, 6 * ma.ne
+    u = np.concatenate([1e-9 * np.exp(rng.uniform(-2, 6, N)), pf.L.reshape(-1, order="F") / 1e-9 * np.exp(rng.uniform(-1, 1, N)),
+                        np.zeros(M), 1e6 * rng.standard_normal(M), np.zeros(N)])
+    ref = oracle.OracleModel(gfs[0], pf, *gfs[1:], pa).ode(u)
+    got = NumpyTwin(gfs[0], pf, *gfs[1:], pa).ode(u)
+    for part in (slice(0, N), slice(N, 2 * N), slice(2 * N, 2 * N + M), slice(2 * N + M, 2 * N + 2 * M), slice(2 * N + 2 * M, None)):
+        np.testing.assert_allclose(got[part], ref[part], rtol=1e-9, atol=1e-12 * np.abs(ref[part]).max())
