@@ -3,8 +3,6 @@
 #pragma once
 #include <cuda_runtime.h>
 
-#include <vector>
-
 #include "gbc_internal.cuh"
 #include "integrator.cuh"
 #include "rhs.cuh"
@@ -77,7 +75,6 @@ struct gbc_model {
     gbc::RawBuf q, qscale, x32, y32, st32, err;
     alignas(128) unsigned char tmap[128];
     gbc::Integrator integ;
-    std::vector<double> hstage;
 
     gbc::RhsArgs args() const {
         gbc::RhsArgs r{};
