@@ -191,11 +191,15 @@ int gbc_integrate_dev(gbc_model* m, double* u_dev, double t0, double t1,
  *   gm row-major (6ne rows, leading dim ldm >= npad + 6ne, even): columns [0,N) hold G12,
  *      [N,npad) zeros and [npad, npad+6ne) G22, with N = nx*nxi and npad = N rounded up to 32;
  *   g21 row-major (N rows, leading dim ld21 >= 6ne, even);
+ *   gm and g21 start on 16-byte boundaries (rows are read as pairs of doubles; GBC_EINVAL
+ *      otherwise, e.g. for a view that starts one double into a larger buffer);
  *   a, b, L, sigma (N), gamma, n (ne); u, du flat states of length 3N + 12ne.
  * The one scratch vector lives in a fixed 8 MiB device array inside the library, so the model
  * must satisfy npad + 6ne <= 1048576 (GBC_EINVAL otherwise). The first call on each device looks
  * the array up (and may load the library's device code): make it before any stream capture.
- * All calls share the array: calls whose work overlaps on the GPU race. stream may be NULL. */
+ * The looked-up address is kept for the life of the process, so do not call this entry point
+ * again on a device after cudaDeviceReset on it. All calls share the array: calls whose work
+ * overlaps on the GPU race. stream may be NULL. */
 int gbc_rhs_visco_noalloc(int nx, int nxi, int ne, const double* st, const double* gm, size_t ldm,
                           const double* g21, size_t ld21, const double* a, const double* b,
                           const double* L, const double* sigma, double eta, double vpl, double f0,

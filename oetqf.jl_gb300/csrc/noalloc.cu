@@ -60,6 +60,10 @@ extern "C" int gbc_rhs_visco_noalloc(int nx, int nxi, int ne, const double* st, 
                                     "1048576 doubles, npad = nx*nxi rounded up to 32)");
     if (ldm < (size_t)(npad + M) || ld21 < (size_t)M || (ldm & 1) || (ld21 & 1))
         return fail(GBC_EINVAL, "gbc_rhs_visco_noalloc: leading dimensions must be even and cover the rows");
+    // the row GEMV reads gm and g21 as 16-byte pairs: an 8-byte-offset view (a slice of a larger
+    // buffer) would be a misaligned access on the device, so refuse it here
+    if ((reinterpret_cast<uintptr_t>(gm) | reinterpret_cast<uintptr_t>(g21)) & 15)
+        return fail(GBC_EINVAL, "gbc_rhs_visco_noalloc: gm and g21 must be 16-byte aligned device pointers");
     if (!(eta > 0) || !(vpl > 0) || !(f0 > 0) || !(v0 > 0))
         return fail(GBC_EINVAL, "gbc_rhs_visco_noalloc: eta, vpl, f0, v0 must be positive");
     double* x = nullptr;

@@ -36,6 +36,20 @@ def test_rejects_models_beyond_the_fixed_scratch():
     assert "fixed scratch" in C.last_error()
 
 
+def test_rejects_misaligned_green_function_rows():
+    """gm and g21 are read as 16-byte pairs; a view starting 8 bytes into a buffer is refused on
+    the host, before any device work (the pointers are never dereferenced)."""
+    from oetqf_gb300 import _capi as C
+    deps0 = np.zeros(6)
+    ok, off = ctypes.c_void_p(256), ctypes.c_void_p(256 + 8)
+    N, ne = 32, 4
+    for gm, g21 in ((off, ok), (ok, off)):
+        rc = C.lib().gbc_rhs_visco_noalloc(4, 8, ne, ok, gm, N + 6 * ne, g21, 6 * ne, ok, ok, ok, ok,
+                                          1.0, 1.0, 0.6, 1e-6, ok, ok, C.ptr(deps0), ok, ok, None)
+        assert rc == -1
+        assert "16-byte aligned" in C.last_error()
+
+
 @pytest.mark.gpu
 def test_noalloc_matches_regular_rhs_twice(oracle):
     torch = pytest.importorskip("torch")
