@@ -123,6 +123,11 @@ int gbc_model_assemble(gbc_model* m, const gbc_fault_mesh* mf, const gbc_hex_mes
                        const double* qcoords, const double* qweights, int nq);
 /* Copy a Green's function back to host memory in the reference layout (parity checks). */
 int gbc_model_export_gf(gbc_model* m, int which, double* host);
+/* Copy chosen rows of GBC_GF12, GBC_GF21 or GBC_GF22 to host memory: rows[k] is a row of the
+ * reference layout (k*ne + j for stress component k at cell j; patch i for GF21), and host receives
+ * nrows x (number of columns) doubles, row by row. For checking entries of large models (the
+ * full 6ne x 6ne block of an 8000-cell mantle is 18 GB) without a full export. */
+int gbc_model_export_gf_rows(gbc_model* m, int which, int nrows, const int* rows, double* host);
 /* Storage precision of the mantle Green's functions (GBC_PREC_*); FP64 by default. BF16/FP16
  * store [G12|G22] and G21 as one 16-bit matrix with an FP32 scale per 128x128 block and
  * accumulate in FP32; the fault-fault kernel runs in FP32 and friction stays FP64. The 16-bit

@@ -460,6 +460,29 @@ int gbc_model_export_gf(gbc_model* m, int which, double* host) {
     return 0;
 }
 
+int gbc_model_export_gf_rows(gbc_model* m, int which, int nrows, const int* rows, double* host) {
+    if (!m || !host || (nrows > 0 && !rows) || nrows < 0) return fail(GBC_EINVAL, "null argument");
+    if (which != GBC_GF12 && which != GBC_GF21 && which != GBC_GF22)
+        return fail(GBC_EINVAL, "row export covers GBC_GF12, GBC_GF21 and GBC_GF22");
+    if (m->ne == 0) return fail(GBC_EINVAL, "fault-only model has no mantle Green's functions");
+    if ((which == GBC_GF12 && !m->has_g12) || (which == GBC_GF21 && !m->has_g21) || (which == GBC_GF22 && !m->has_g22))
+        return fail(GBC_ESTATE, "Green's function not set");
+    // the device keeps these blocks row-major with the reference's row numbering, so a row is one
+    // contiguous run: G12 row r = gm[r, 0:N), G22 row r = gm[r, npad:npad+M), G21 row i = g21[i, 0:M)
+    const long long R = (which == GBC_GF21) ? m->N : m->M;
+    const long long C = (which == GBC_GF12) ? m->N : m->M;
+    const double* src = (which == GBC_GF21) ? m->g21.p : (which == GBC_GF12) ? m->gm.p : m->gm.p + m->npad;
+    const size_t ld = (which == GBC_GF21) ? m->ld21 : m->ldm;
+    for (int k = 0; k < nrows; ++k)
+        if (rows[k] < 0 || rows[k] >= R) return fail(GBC_EINVAL, "row index out of range");
+    cudaStream_t s = m->stream;
+    for (int k = 0; k < nrows; ++k)
+        GBC_CUDA(cudaMemcpyAsync(host + (size_t)k * C, src + (size_t)rows[k] * ld, sizeof(double) * C,
+                                 cudaMemcpyDeviceToHost, s));
+    GBC_CUDA(cudaStreamSynchronize(s));
+    return 0;
+}
+
 int gbc_model_assemble(gbc_model* m, const gbc_fault_mesh* mf, const gbc_hex_mesh* ma, double lambda, double mu,
                        int ftype, int nrept, double buffer_ratio, const double* qcoords, const double* qweights,
                        int nq) {

@@ -71,6 +71,7 @@ def lib():
             "gbc_model_set_gf": [P, I, PD],
             "gbc_model_assemble": [P, ctypes.POINTER(FaultMesh), ctypes.POINTER(HexMesh), D, D, I, I, D, PD, PD, I],
             "gbc_model_export_gf": [P, I, PD],
+            "gbc_model_export_gf_rows": [P, I, I, ctypes.POINTER(I), PD],
             "gbc_model_set_precision": [P, I],
             "gbc_rhs": [P, D, ctypes.POINTER(PD), ctypes.POINTER(PD), I],
             "gbc_rhs_dev": [P, D, P, P],

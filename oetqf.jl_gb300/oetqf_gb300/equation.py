@@ -149,6 +149,15 @@ class GB300Model:
         C.check(C.lib().gbc_model_export_gf(self.h, which, C.ptr(out)))
         return out.reshape(shape[which], order="F")
 
+    def export_gf_rows(self, which: int, rows) -> np.ndarray:
+        """Chosen rows of GBC_GF12 / GBC_GF21 / GBC_GF22 in the reference layout's numbering
+        (k*ne + j for stress component k at cell j; patch i for GF21): array (len(rows), columns)."""
+        r = np.ascontiguousarray(rows, dtype=np.int32)
+        cols = self.N if which == C.GBC_GF12 else 6 * self.ne
+        out = np.zeros(r.size * cols)
+        C.check(C.lib().gbc_model_export_gf_rows(self.h, which, r.size, r.ctypes.data_as(ctypes.POINTER(C.I)), C.ptr(out)))
+        return out.reshape(r.size, cols)
+
     def set_precision(self, mode: int):
         C.check(C.lib().gbc_model_set_precision(self.h, mode))
 

@@ -63,6 +63,15 @@ int orc_gf_mm(const orc_hex_mesh* ma, double lambda, double mu, const double* qc
 /* rfft of the symmetric circulant embedding [st[:,j,l]; reverse(st[2:end,j,l])]
  * (src/BEM/GF.jl:60-67): out is complex interleaved (re,im) of shape (nx,nxi,nxi). */
 void orc_gf_ff_dft(int nx, int nxi, const double* st, double* st_dft);
+/* receiver subsets of the three mantle Green's functions (rows in the reference layout, out
+ * row-major: fault->mantle (6*nr, N), mantle->fault (nr, 6ne), mantle-mantle (6*nr, 6ne)) */
+int orc_gf_fm_rows(const orc_fault_mesh* mf, const orc_hex_mesh* ma, double lambda, double mu,
+                   int ftype, int nrept, double buffer_ratio, const double* qc, const double* qw,
+                   int nq, int nr, const int* recv, double* out);
+int orc_gf_mf_rows(const orc_hex_mesh* ma, const orc_fault_mesh* mf, double lambda, double mu,
+                   int ftype, int nr, const int* recv, double* out);
+int orc_gf_mm_rows(const orc_hex_mesh* ma, double lambda, double mu, const double* qc,
+                   const double* qw, int nq, int nr, const int* recv, double* out);
 
 /* Right-hand side of src/BEM/equation.jl. gf_dft is the complex (nx,nxi,nxi) kernel. */
 typedef struct {

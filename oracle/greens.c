@@ -195,3 +195,94 @@ int orc_gf_mm(const orc_hex_mesh* ma, double lambda, double mu, const double* qc
     }
     return 0;
 }
+
+/* ---- receiver subsets (the same loops as above restricted to chosen receivers) -------------
+ * For parity checks of device-assembled Green's functions at sizes where the full matrices are
+ * too costly for the oracle. Rows are the reference layout's rows: fault->mantle and
+ * mantle-mantle row (k, j) = k*ne + j (stress component k at cell j), mantle->fault row i (patch i).
+ * out is row-major: one output row per requested reference row, all sources in the reference's
+ * column order. */
+
+/* fault -> mantle rows of receiver cells recv[0..nr) (GF.jl:123-174); out (6*nr, N) */
+int orc_gf_fm_rows(const orc_fault_mesh* mf, const orc_hex_mesh* ma, double lambda, double mu,
+                   int ftype, int nrept, double buffer_ratio, const double* qc, const double* qw,
+                   int nq, int nr, const int* recv, double* out) {
+    if (buffer_ratio < 0) return -1;
+    const int nx = mf->nx, ndisl = mf->nx * mf->nxi;
+    const double lrept = (buffer_ratio + 1.0) * (mf->dx * nx);
+    const double alpha = (lambda + mu) / (lambda + 2.0 * mu);
+    const double ud1 = ftype == 0 ? 1.0 : 0.0, ud2 = ftype == 0 ? 0.0 : 1.0;
+    memset(out, 0, sizeof(double) * 6 * (size_t)nr * ndisl);
+#pragma omp parallel for schedule(dynamic) collapse(2)
+    for (int r = 0; r < nr; ++r)
+        for (int j = 0; j < ndisl; ++j) {
+            const int i = recv[r], q1 = j % nx, q2 = j / nx;
+            double u[12], acc[12], s[6] = {0, 0, 0, 0, 0, 0};
+            for (int w = 0; w < nq; ++w) {
+                double rx = ma->cx[i] + qc[3 * w] * ma->dx[i] / 2.0;
+                double ry = ma->cy[i] + qc[3 * w + 1] * ma->dy[i] / 2.0;
+                double rz = ma->cz[i] + qc[3 * w + 2] * ma->dz[i] / 2.0;
+                memset(acc, 0, sizeof(acc));
+                for (int p = -nrept; p <= nrept; ++p) {
+                    double jump = p * lrept;
+                    orc_dc3d(rx, ry, rz, alpha, mf->dep, mf->dip, mf->ax[2 * q1] + jump,
+                             mf->ax[2 * q1 + 1] + jump, mf->axi[2 * q2], mf->axi[2 * q2 + 1],
+                             ud1, ud2, 0.0, u);
+                    for (int k = 0; k < 12; ++k) acc[k] += u[k];
+                }
+                double lekk = lambda * (acc[3] + acc[7] + acc[11]);
+                s[0] += qw[w] * (lekk + 2.0 * mu * acc[3]);
+                s[1] += qw[w] * (mu * (acc[4] + acc[6]));
+                s[2] += qw[w] * (mu * (acc[5] + acc[9]));
+                s[3] += qw[w] * (lekk + 2.0 * mu * acc[7]);
+                s[4] += qw[w] * (mu * (acc[8] + acc[10]));
+                s[5] += qw[w] * (lekk + 2.0 * mu * acc[11]);
+            }
+            for (int k = 0; k < 6; ++k) out[((size_t)r * 6 + k) * ndisl + j] = s[k];
+        }
+    return 0;
+}
+
+/* mantle -> fault rows of receiver patches recv[0..nr) (GF.jl:194-227); out (nr, 6ne) */
+int orc_gf_mf_rows(const orc_hex_mesh* ma, const orc_fault_mesh* mf, double lambda, double mu,
+                   int ftype, int nr, const int* recv, double* out) {
+    const int ne = ma->ne, nx = mf->nx;
+    const size_t M = 6 * (size_t)ne;
+    const double nu = lambda / 2.0 / (lambda + mu);
+#pragma omp parallel for schedule(dynamic) collapse(2)
+    for (int r = 0; r < nr; ++r)
+        for (int j = 0; j < ne; ++j) {
+            double s66[6][6];
+            const int i = recv[r], q1 = i % nx, q2 = i / nx;
+            orc_hex8_unit_stresses(s66, mf->x[q1], mf->y[q2], mf->z[q2], ma->qx[j], ma->qy[j],
+                                   ma->qz[j], ma->dx[j], ma->dy[j], ma->dz[j], mu, nu);
+            for (int p = 0; p < 6; ++p) out[(size_t)r * M + (size_t)p * ne + j] = traction_vol(ftype, s66[p], mf->dip);
+        }
+    return 0;
+}
+
+/* mantle-mantle rows of receiver cells recv[0..nr) (GF.jl:250-290); out (6*nr, 6ne) */
+int orc_gf_mm_rows(const orc_hex_mesh* ma, double lambda, double mu, const double* qc,
+                   const double* qw, int nq, int nr, const int* recv, double* out) {
+    const int ne = ma->ne;
+    const size_t M = 6 * (size_t)ne;
+    const double nu = lambda / 2.0 / (lambda + mu);
+    memset(out, 0, sizeof(double) * 6 * (size_t)nr * M);
+#pragma omp parallel for schedule(dynamic) collapse(2)
+    for (int r = 0; r < nr; ++r)
+        for (int i = 0; i < ne; ++i) {  /* source */
+            double s66[6][6];
+            const int j = recv[r];      /* receiver */
+            for (int q = 0; q < nq; ++q) {
+                double rx = ma->cx[j] + qc[3 * q] * ma->dx[j] / 2.0;
+                double ry = ma->cy[j] + qc[3 * q + 1] * ma->dy[j] / 2.0;
+                double rz = ma->cz[j] + qc[3 * q + 2] * ma->dz[j] / 2.0;
+                orc_hex8_unit_stresses(s66, rx, ry, rz, ma->qx[i], ma->qy[i], ma->qz[i], ma->dx[i],
+                                       ma->dy[i], ma->dz[i], mu, nu);
+                for (int p = 0; p < 6; ++p)
+                    for (int k = 0; k < 6; ++k)
+                        out[((size_t)r * 6 + k) * M + (size_t)p * ne + i] += s66[p][k] * qw[q];
+            }
+        }
+    return 0;
+}

@@ -79,6 +79,11 @@ def lib():
             L.orc_gf_fm.argtypes = [ctypes.POINTER(FaultMesh), ctypes.POINTER(HexMesh), D, D, I, I, D, PD, PD, I, PD]
             L.orc_gf_mf.argtypes = [ctypes.POINTER(HexMesh), ctypes.POINTER(FaultMesh), D, D, I, PD]
             L.orc_gf_mm.argtypes = [ctypes.POINTER(HexMesh), D, D, PD, PD, I, PD]
+            PI = ctypes.POINTER(ctypes.c_int)
+            L.orc_gf_fm_rows.argtypes = [ctypes.POINTER(FaultMesh), ctypes.POINTER(HexMesh), D, D, I, I, D, PD, PD, I, I,
+                                         PI, PD]
+            L.orc_gf_mf_rows.argtypes = [ctypes.POINTER(HexMesh), ctypes.POINTER(FaultMesh), D, D, I, I, PI, PD]
+            L.orc_gf_mm_rows.argtypes = [ctypes.POINTER(HexMesh), D, D, PD, PD, I, I, PI, PD]
             L.orc_ode_fault.argtypes = [ctypes.POINTER(Model)] + [PD] * 5
             L.orc_ode_visco.argtypes = [ctypes.POINTER(Model)] + [PD] * 8
             L.orc_ode_dilatancy.argtypes = [ctypes.POINTER(Model)] + [PD] * 7
@@ -184,6 +189,50 @@ def gf_mm(ma, lam, mu, quad=None):
     hs = hex_struct(ma, keep)
     lib().orc_gf_mm(ctypes.byref(hs), lam, mu, _p(qc), _p(qw), len(qw), _p(st))
     return st.reshape((6 * ma.ne, 6 * ma.ne), order="F")
+
+
+def _ints(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def gf_fm_rows(mf, ma, lam, mu, cells, ftype=0, nrept=2, buffer_ratio=0.0, quad=None):
+    """Rows (k*ne + j for k in 0..5) of the fault->mantle Green's function for receiver cells j in
+    `cells`: array (len(cells), 6, N)."""
+    keep = _Keep()
+    qc, qw = quad if quad is not None else (np.zeros(3), np.ones(1))
+    qc, qw = _c(qc), _c(qw)
+    r = _ints(cells)
+    out = np.zeros(6 * r.size * mf.nx * mf.nξ)
+    fs, hs = fault_struct(mf, keep), hex_struct(ma, keep)
+    if lib().orc_gf_fm_rows(ctypes.byref(fs), ctypes.byref(hs), lam, mu, ftype, nrept, buffer_ratio, _p(qc), _p(qw),
+                            len(qw), r.size, r.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _p(out)) != 0:
+        raise AssertionError("Argument `buffer_ratio` must be ≥ 0.")
+    return out.reshape(r.size, 6, mf.nx * mf.nξ)
+
+
+def gf_mf_rows(ma, mf, lam, mu, patches, ftype=0):
+    """Rows of the mantle->fault Green's function for receiver patches: array (len(patches), 6ne)."""
+    keep = _Keep()
+    r = _ints(patches)
+    out = np.zeros(r.size * 6 * ma.ne)
+    fs, hs = fault_struct(mf, keep), hex_struct(ma, keep)
+    lib().orc_gf_mf_rows(ctypes.byref(hs), ctypes.byref(fs), lam, mu, ftype, r.size,
+                         r.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _p(out))
+    return out.reshape(r.size, 6 * ma.ne)
+
+
+def gf_mm_rows(ma, lam, mu, cells, quad=None):
+    """Rows (k*ne + j for k in 0..5) of the mantle-mantle Green's function for receiver cells j in
+    `cells`: array (len(cells), 6, 6ne)."""
+    keep = _Keep()
+    qc, qw = quad if quad is not None else (np.zeros(3), np.ones(1))
+    qc, qw = _c(qc), _c(qw)
+    r = _ints(cells)
+    out = np.zeros(r.size * 36 * ma.ne)
+    hs = hex_struct(ma, keep)
+    lib().orc_gf_mm_rows(ctypes.byref(hs), lam, mu, _p(qc), _p(qw), len(qw), r.size,
+                         r.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _p(out))
+    return out.reshape(r.size, 6, 6 * ma.ne)
 
 
 class OracleModel:

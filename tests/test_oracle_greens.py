@@ -103,3 +103,21 @@ def test_reciprocity_fault_mantle(oracle):
         S = lam * np.trace(G) * np.eye(3) + mu * (G + G.T)
         rhs += qw[q] * V * np.array([S[0, 0], 2 * S[0, 1], 2 * S[0, 2], S[1, 1], 2 * S[1, 2], S[2, 2]])
     np.testing.assert_allclose(lhs, rhs, rtol=1e-6, atol=1e-6 * np.abs(rhs).max())
+
+
+def test_receiver_rows_equal_the_full_blocks(oracle):
+    """The receiver-subset routines (used to check the 8000-cell mantle on the GPU) run the same
+    loops as the full blocks: their rows are bit for bit the full blocks' rows."""
+    from oetqf_gb300 import gen_hex8_box, gen_mesh
+    mf = gen_mesh("RectOkada", 100.0, 100.0, 10.0, 20.0, 90.0)
+    ma = gen_hex8_box(-100.0, -50.0, -20.0, 200.0, 100.0, -30.0, 2, 3, 4)
+    g12, g21, g22 = oracle.gf_fm(mf, ma, 1.0, 1.0), oracle.gf_mf(ma, mf, 1.0, 1.0), oracle.gf_mm(ma, 1.0, 1.0)
+    ne, cells, patches = ma.ne, [0, 5, 23], [0, 7, mf.nx * mf.nξ - 1]
+    r12, r22 = oracle.gf_fm_rows(mf, ma, 1.0, 1.0, cells), oracle.gf_mm_rows(ma, 1.0, 1.0, cells)
+    for a, j in enumerate(cells):
+        for k in range(6):
+            assert np.array_equal(r12[a, k], g12[k * ne + j])
+            assert np.array_equal(r22[a, k], g22[k * ne + j])
+    r21 = oracle.gf_mf_rows(ma, mf, 1.0, 1.0, patches)
+    for a, i in enumerate(patches):
+        assert np.array_equal(r21[a], g21[i])
