@@ -142,6 +142,8 @@ int gbc_model_set_log_theta(gbc_model* m, int on);
 /* Device error word of the model's bounded waits (0 = none); nonzero means a TMA pipeline wait
  * timed out and the last right-hand side is not valid. */
 int gbc_model_error_word(gbc_model* m);
+/* Resets the error word to 0 (after the caller has handled a timeout). */
+int gbc_model_clear_error_word(gbc_model* m);
 
 /* ode(du, u, p, t) (equation.jl:156-166 / 168-183 / 185-205) on host buffers in ArrayPartition
  * order: nparts = 3: (v, θ, δ), each (nx,nxi); 4 with dilatancy: (v, θ, δ, 𝓅);
@@ -364,6 +366,19 @@ int gbc_server_set_gf_cache(gbc_server* s, int enabled);
 void gbc_server_destroy(gbc_server* s);
 
 /* ---- Diagnostics ------------------------------------------------------------------------ */
+/* No reference counterpart: failure injection for tests of the bounded waits. mode 1 makes every
+ * 16-bit (GBC_PREC_BF16/F16) mantle GEMV launched afterwards on the current device issue no TMA
+ * copies and give up each pipeline wait after 1024 polls, so every such right-hand side takes its
+ * timeout path: it records the model's error word and returns, with no copy in flight, and its
+ * output is not valid. mode 0 (the default) restores normal operation. Not for production use. */
+int gbc_debug_pipeline_fault(int mode);
+/* No reference counterpart: a throughput probe of the GPU's FP64 FMA pipe, the bound of the FP64
+ * row GEMV on this chip. Launches blocks x threads threads (threads a multiple of 32, <= 1024), each
+ * running independent FMA chains for iters iterations on `stream`, and writes one double per thread
+ * to out_dev (device, blocks*threads doubles). *flops receives the launch's FLOP count (2 per
+ * FMA); time the launch with CUDA events on the same stream. Does not synchronise. */
+int gbc_probe_fp64_fma(double* out_dev, int blocks, int threads, long long iters, void* stream,
+                       double* flops);
 int gbc_last_error(char* buf, size_t len);
 const char* gbc_version(void);
 /* Number of kernels this library launched in this process (used to report GPU launch counts). */

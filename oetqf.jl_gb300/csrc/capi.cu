@@ -541,6 +541,19 @@ int gbc_model_error_word(gbc_model* m) {
     return h;
 }
 
+int gbc_model_clear_error_word(gbc_model* m) {
+    if (!m) return fail(GBC_EINVAL, "null model");
+    if (!m->err.p) return 0;
+    GBC_CUDA(cudaMemsetAsync(m->err.p, 0, sizeof(int), m->stream));
+    GBC_CUDA(cudaStreamSynchronize(m->stream));
+    return 0;
+}
+
+int gbc_debug_pipeline_fault(int mode) {
+    if (mode != 0 && mode != 1) return fail(GBC_EINVAL, "gbc_debug_pipeline_fault: mode must be 0 or 1");
+    return set_pipeline_fault(mode);
+}
+
 int gbc_rhs_dev(gbc_model* m, double t, const double* u, double* du) {
     (void)t;
     if (!m || !u || !du) return fail(GBC_EINVAL, "null argument");

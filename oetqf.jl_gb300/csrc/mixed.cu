@@ -136,6 +136,19 @@ int encode_qmap(int mode, void* q, long long rowsq, long long ldq, void* tmap_ou
                           rowsq, ldq, TC, TR, false, tmap_out);
 }
 
+// Failure-injection hook for tests (gbc_debug_pipeline_fault): when set, the GEMV's producer
+// issues no copies, so no full-barrier phase ever completes, and every pipeline wait gives up after
+// kFaultPolls polls. The kernel then takes its timeout path (error word, return) without any copy
+// in flight. Zero (the default) leaves the kernel as it is.
+__device__ int g_pipeline_fault = 0;
+constexpr long long kFaultPolls = 1024;
+
+__device__ __forceinline__ bool mbar_wait_n(uint64_t* bar, unsigned parity, long long polls) {
+    for (long long i = 0; i < polls; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
 // y = Q x for one 32-row tile per CTA; mantle rows go to du (FP64), fault rows to y32.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_gemv_tma(const __grid_constant__ CUtensorMap tm, RhsArgs a,
@@ -158,8 +171,10 @@ __global__ void __launch_bounds__(256) k_gemv_tma(const __grid_constant__ CUtens
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
+    const bool inject = g_pipeline_fault != 0;
+    const long long polls = inject ? kFaultPolls : kWaitLimit;
     const bool producer = (threadIdx.x == 0);
-    if (producer) {
+    if (producer && !inject) {
         for (int c = 0; c < STAGES && c < nch; ++c) {
             mbar_expect_tx(&full[c], kTileBytes + kXBytes);
             tma_tile(tiles + c * kTileBytes, &tm, c * TC, (int)row0, &full[c]);
@@ -173,7 +188,7 @@ __global__ void __launch_bounds__(256) k_gemv_tma(const __grid_constant__ CUtens
     for (; c < nch; ++c) {
         const int s = c % STAGES;
         const unsigned ph = (unsigned)((c / STAGES) & 1);
-        if (!mbar_wait(&full[s], ph)) { ok = false; break; }
+        if (!mbar_wait_n(&full[s], ph, polls)) { ok = false; break; }
         const unsigned char* tile = tiles + s * kTileBytes;
         const float4* xv = reinterpret_cast<const float4*>(xs + s * TC) + 2 * lane;
         const float4 x0 = xv[0], x1 = xv[1];
@@ -196,7 +211,7 @@ __global__ void __launch_bounds__(256) k_gemv_tma(const __grid_constant__ CUtens
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);
         if (producer && c + STAGES < nch) {
-            if (!mbar_wait(&empty[s], ph)) { ok = false; break; }
+            if (!mbar_wait_n(&empty[s], ph, polls)) { ok = false; break; }
             mbar_expect_tx(&full[s], kTileBytes + kXBytes);
             tma_tile(tiles + s * kTileBytes, &tm, (c + STAGES) * TC, (int)row0, &full[s]);
             bulk_copy(xs + s * TC, a.x32 + (size_t)(c + STAGES) * TC, kXBytes, &full[s]);
@@ -204,7 +219,7 @@ __global__ void __launch_bounds__(256) k_gemv_tma(const __grid_constant__ CUtens
     }
     if (!ok) {
         atomicExch(a.err, 1);
-        if (producer) {  // let our own copies in flight land before the CTA's shared memory goes away
+        if (producer && !inject) {  // let our own copies in flight land before the CTA's shared memory goes away
             for (int k = c; k < nch && k < c + STAGES; ++k) mbar_wait(&full[k % STAGES], (unsigned)((k / STAGES) & 1));
         }
         return;
@@ -286,6 +301,12 @@ __global__ void __launch_bounds__(kFR_II * kFR_L) k_fault_rows_smem(RhsArgs a, c
 }
 
 size_t fault_rows_smem_bytes(int N, int nx, int nxi) { return sizeof(float) * ((size_t)N + (size_t)nx * nxi); }
+
+int set_pipeline_fault(int mode) {
+    const int v = mode ? 1 : 0;
+    GBC_CUDA(cudaMemcpyToSymbol(g_pipeline_fault, &v, sizeof(int)));
+    return 0;
+}
 
 int launch_rhs_mixed(const RhsArgs& a, const double* u, double* du, cudaStream_t s) {
     const StateLayout L = layout_of(a.N, a.ne);

@@ -128,6 +128,8 @@ int rhs_kernel_count(const RhsArgs& a);
 
 // Block-scaled 16-bit path (mixed.cu)
 int launch_rhs_mixed(const RhsArgs& a, const double* u, double* du, cudaStream_t s);
+// failure-injection hook of the 16-bit GEMV pipeline on the current device (gbc_debug_pipeline_fault)
+int set_pipeline_fault(int mode);
 // Builds q and qscale from the FP64 rows (gm with ldm, g21 with ld21) on stream s.
 int quantize_mantle(int mode, int N, int npad, long long M, long long Mpad, long long rowsq, long long ldq,
                     const double* gm, size_t ldm, const double* g21, size_t ld21, void* q, float* qscale,

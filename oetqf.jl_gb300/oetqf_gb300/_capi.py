@@ -103,6 +103,9 @@ def lib():
             "gbc_sweep_integrate": [P, PD, D, D, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
             "gbc_sweep_integrate_dev": [P, P, D, D, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
             "gbc_sweep_error_word": [P],
+            "gbc_probe_fp64_fma": [P, I, I, LL, P, PD],
+            "gbc_model_clear_error_word": [P],
+            "gbc_debug_pipeline_fault": [I],
         }
         for name, args in sig.items():
             f = getattr(L, name)

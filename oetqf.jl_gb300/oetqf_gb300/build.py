@@ -12,7 +12,7 @@ CSRC = os.path.join(TREE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(TREE), "include")
 LIBDIR = os.path.join(TREE, "lib")
 LIB = os.path.join(LIBDIR, "libgbcycle.so")
-SOURCES = ["gf_kernels.cu", "rhs_kernels.cu", "integrator.cu", "capi.cu", "noalloc.cu", "mixed.cu", "df64.cu", "ensemble.cu", "serve.cu", "sweep.cu"]
+SOURCES = ["gf_kernels.cu", "rhs_kernels.cu", "integrator.cu", "capi.cu", "noalloc.cu", "mixed.cu", "df64.cu", "ensemble.cu", "serve.cu", "sweep.cu", "probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
 

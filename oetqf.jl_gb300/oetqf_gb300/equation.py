@@ -167,6 +167,9 @@ class GB300Model:
     def error_word(self) -> int:
         return int(C.lib().gbc_model_error_word(self.h))
 
+    def clear_error_word(self) -> None:
+        C.check(C.lib().gbc_model_clear_error_word(self.h))
+
     # -- right-hand side --------------------------------------------------------------------------
     def rhs(self, du: ArrayPartition, u: ArrayPartition, t: float = 0.0):
         n = len(u.x)

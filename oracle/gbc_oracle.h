@@ -128,6 +128,17 @@ int orc_integrate_record(const orc_model* m, double* u, double t0, double t1, co
                          orc_solver_stats* st, int stride, long long max_records, double* t_out,
                          double* u_out, long long* nrec);
 int orc_num_threads(void);
+
+/* Timed-baseline variant (fastconv.c): the same Toeplitz traction rate through radix-2 FFTs of
+ * length P >= 2nx - 1 (H: the real spectra of the even kernel columns, P x nxi x nxi), and many
+ * models integrated in parallel, one model per host thread, optionally with that convolution. */
+typedef struct { int P, nx, nxi; double* H; } orc_fftconv;
+extern _Thread_local const orc_fftconv* orc_tl_fastconv;
+int orc_fftconv_init(const orc_model* m, orc_fftconv* c);
+void orc_fftconv_free(orc_fftconv* c);
+void orc_dtau_dt_fft(const orc_fftconv* c, const orc_model* m, const double* v, double* dtau);
+int orc_integrate_many(const orc_model* const* ms, int nm, double* const* us, const double* t0, const double* t1,
+                       const orc_solver_opts* o, orc_solver_stats* st, int fft, int nthreads);
 /* The VCABM step coefficients psi (k), beta (k) and Adams weights g_0..g_k for order k and step h
  * given psi_prev (the previous step's psi); exposed for tests. */
 void orc_abm_coefficients(int k, double h, const double* psi_prev, double* psi, double* beta, double* g);

@@ -28,8 +28,13 @@ static void tw_get(int n) {
     tw.n = n;
 }
 
-/* relative_velocity! + dtau_dt! (equation.jl:35-61): dtau (nx,nxi) from v */
+/* relative_velocity! + dtau_dt! (equation.jl:35-61): dtau (nx,nxi) from v. A thread integrating
+ * under orc_integrate_many with fft on takes the FFT variant of fastconv.c instead. */
 void orc_dtau_dt(const orc_model* m, const double* v, double* dtau) {
+    if (orc_tl_fastconv) {
+        orc_dtau_dt_fft(orc_tl_fastconv, m, v, dtau);
+        return;
+    }
     const int nx = m->nx, nxi = m->nxi, n = 2 * nx - 1;
     tw_get(n);
     const double* cs = tw.cs;  /* the calling thread's tables (they are thread-local) */

@@ -42,6 +42,10 @@ class Model(ctypes.Structure):
                 ("gf11_dft", PD), ("gf12", PD), ("gf21", PD), ("gf22", PD)]
 
 
+class FFTConv(ctypes.Structure):
+    _fields_ = [("P", I), ("nx", I), ("nxi", I), ("H", PD)]
+
+
 ALGS = {"Tsit5": 0, "VCABM5": 1}
 
 
@@ -57,7 +61,7 @@ class SolverStats(ctypes.Structure):
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc, OpenMP)."""
-    srcs = [os.path.join(HERE, f) for f in ("okada_dc3d.c", "hex8_volume.c", "greens.c", "ode.c", "gbc_oracle.h")]
+    srcs = [os.path.join(HERE, f) for f in ("okada_dc3d.c", "hex8_volume.c", "greens.c", "ode.c", "fastconv.c", "gbc_oracle.h", "Makefile")]
     stale = not os.path.exists(LIB_PATH) or any(os.path.getmtime(s) > os.path.getmtime(LIB_PATH) for s in srcs)
     if force or stale:
         subprocess.run(["make", "-s", "-C", HERE], check=True)
@@ -94,6 +98,13 @@ def lib():
                                                ctypes.POINTER(ctypes.c_longlong)]
             L.orc_integrate_record.restype = I
             L.orc_gl_table.argtypes = [I, PD, PD]
+            L.orc_fftconv_init.argtypes = [ctypes.POINTER(Model), ctypes.POINTER(FFTConv)]
+            L.orc_fftconv_init.restype = I
+            L.orc_fftconv_free.argtypes = [ctypes.POINTER(FFTConv)]
+            L.orc_dtau_dt_fft.argtypes = [ctypes.POINTER(FFTConv), ctypes.POINTER(Model), PD, PD]
+            L.orc_integrate_many.argtypes = [ctypes.POINTER(ctypes.POINTER(Model)), I, ctypes.POINTER(PD), PD, PD,
+                                             ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats), I, I]
+            L.orc_integrate_many.restype = I
             L.orc_num_threads.restype = I
             L.orc_dtau_dt.argtypes = [ctypes.POINTER(Model), PD, PD]
             L.orc_tsit5_tableau.argtypes = [PD, PD]
@@ -303,6 +314,38 @@ class OracleModel:
         s = SolverStats()
         lib().orc_integrate(ctypes.byref(self.m), _p(u), t0, t1, ctypes.byref(o), ctypes.byref(s))
         return u, s
+
+
+def dtau_dt_fft(om, v):
+    """The traction rate of om.dtau_dt through the FFT variant (fastconv.c) used for timing."""
+    c = FFTConv()
+    if lib().orc_fftconv_init(ctypes.byref(om.m), ctypes.byref(c)) != 0:
+        raise MemoryError("fftconv tables")
+    v = _c(np.asarray(v).reshape(-1, order="F"))
+    out = np.zeros_like(v)
+    lib().orc_dtau_dt_fft(ctypes.byref(c), ctypes.byref(om.m), _p(v), _p(out))
+    lib().orc_fftconv_free(ctypes.byref(c))
+    return out
+
+
+def integrate_many(models, u0s, t0, t1, reltol=1e-6, abstol=1e-8, dt0=1e-8, dtmax=np.inf, dtmin=1e-14,
+                   maxiters=10**9, alg="Tsit5", fft=True, threads=None):
+    """Independent fault-only or viscoelastic oracle models integrated in parallel, one model per
+    host thread (orc_integrate_many); with fft the traction rate goes through the FFT variant.
+    Returns (list of final states, list of stats)."""
+    n = len(models)
+    mantle = 1 if models[0].ne else 0
+    us = [_c(u).copy() for u in u0s]
+    ptrs = (PD * n)(*[_p(u) for u in us])
+    mp = (ctypes.POINTER(Model) * n)(*[ctypes.pointer(om.m) for om in models])
+    a0 = _c(np.broadcast_to(t0, (n,)))
+    a1 = _c(np.broadcast_to(t1, (n,)))
+    o = SolverOpts(reltol, abstol, dt0, dtmax, dtmin, maxiters, mantle, ALGS[alg])
+    st = (SolverStats * n)()
+    if lib().orc_integrate_many(mp, n, ptrs, _p(a0), _p(a1), ctypes.byref(o), st, int(bool(fft)),
+                                int(threads or num_threads())) != 0:
+        raise MemoryError("fftconv tables")
+    return us, list(st)
 
 
 def integrate_record(om, u0, t0, t1, stride, max_records, reltol=1e-6, abstol=1e-8, dt0=1e-8, dtmax=np.inf,

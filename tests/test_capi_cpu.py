@@ -55,3 +55,9 @@ def test_invalid_arguments_rejected_before_device_use():
     h = ctypes.c_void_p()
     assert C.lib().gbc_model_create(0, 2, 0, ctypes.byref(h)) == -1
     assert C.lib().gbc_model_create(2, 2, -1, ctypes.byref(h)) == -1
+
+
+def test_failure_injection_hook_checks_its_mode_before_any_device_use():
+    from oetqf_gb300 import _capi as C
+    assert C.lib().gbc_debug_pipeline_fault(7) == -1
+    assert "mode" in C.last_error()
