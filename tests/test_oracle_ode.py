@@ -272,3 +272,27 @@ def test_vcabm5_viscoelastic_matches_scipy(oracle):
     np.testing.assert_allclose(u1[:N], ref.y[:N, -1], rtol=1e-7)
     np.testing.assert_allclose(u1[N:2 * N], ref.y[N:2 * N, -1], rtol=1e-7)
     np.testing.assert_allclose(u1[2 * N + 6 * ne:], ref.y[2 * N + 6 * ne:, -1], rtol=1e-6, atol=1e-6 * np.abs(ref.y[2 * N + 6 * ne:, -1]).max())
+
+
+def test_fft_convolution_variant_equals_the_direct_transform(oracle):
+    """The timed-baseline traction rate (radix-2 FFTs of length 2^k >= 2nx - 1) equals the
+    checker's direct transforms of length 2nx - 1 (equation.jl:44-61) to round-off, for odd and
+    even depth counts, and member-parallel integration changes nothing else."""
+    from oetqf_gb300.workloads import YEAR, fault_ensemble
+    ms = fault_ensemble(n_models=3, years=0.05, n_range=(60, 400), seed=41, nxi=7)
+    oms = [oracle.OracleModel(oracle.gf_ff(m.mf, m.lam, m.mu, fourier=True), m.pf) for m in ms]
+    rng = np.random.default_rng(3)
+    for m, om in zip(ms, oms):
+        v = m.pf.vpl * np.exp(rng.uniform(-2, 8, m.N))
+        a, b = om.dtau_dt(v), oracle.dtau_dt_fft(om, v)
+        assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max()
+    S = dict(reltol=1e-6, abstol=1e-8, dt0=1e-8, dtmax=0.2 * YEAR, alg="VCABM5")
+    seq = [om.integrate(m.u0, 0.0, 0.05 * YEAR, **S) for m, om in zip(ms, oms)]
+    par, st = oracle.integrate_many(oms, [m.u0 for m in ms], 0.0, 0.05 * YEAR, fft=False, threads=2, **S)
+    for (u1, s1), u2, s2 in zip(seq, par, st):
+        np.testing.assert_array_equal(u1, u2)
+        assert s1.nrhs == s2.nrhs
+    fast, st = oracle.integrate_many(oms, [m.u0 for m in ms], 0.0, 0.05 * YEAR, fft=True, threads=2, **S)
+    for (u1, _), u2, s2 in zip(seq, fast, st):
+        assert s2.status == 0
+        assert np.abs(u1 - u2).max() <= 1e-9 * np.abs(u1).max()
