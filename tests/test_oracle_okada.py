@@ -4,6 +4,8 @@ The reference's dc3d lives in GeoGreensFunctions.jl (not vendored, no golden vec
 src/BEM/GF.jl:49-53 and :156-160. These tests pin the C restatement by
   * 40-digit known answers (tests/golden/okada_golden.json, made by make_golden.py),
   * an independent formula set: Okada (1985) surface displacement,
+  * an independent solution: Volterra's surface integral of Kelvin's full-space point-force solution
+    (the deep limit of a finite rectangle),
   * equilibrium, the traction-free surface, the slip jump, far-field decay.
 """
 import json
@@ -116,3 +118,44 @@ def test_edge_and_above_surface(oracle):
     # receiver on the fault edge (q = 0, eta = 0 inside the strike range)
     u, rc = oracle.dc3d(0.0, 0.0, -1.0, 2 / 3, 1.0, 90.0, -1, 1, -1, 0, 1, 0, 0)
     assert rc == 1 and not np.any(u)
+
+
+@pytest.mark.parametrize("dip", [90.0, 37.0])
+@pytest.mark.parametrize("r", [(0.5, 0.7, 0.3), (1.4, -0.4, -0.2), (-0.6, 1.5, 1.0)])
+def test_deep_rectangle_matches_the_kelvin_surface_integral(oracle, dip, r):
+    """An independent pin of dc3d's displacement gradient: far below the free surface a finite
+    rectangular dislocation tends to its full-space field, Volterra's surface integral of Kelvin's
+    point-force solution, u_i,l = -int_S (C : sym(b n))_jk G_ij,kl dS with n = s x d (strike s,
+    up-dip d) and b = U1 s + U2 d + U3 n -- formulas that share nothing with Okada's. At 16 km depth
+    for a 2 x 1.5 rectangle the two agree to ~1e-12 (the gap scales as depth^-3)."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from test_oracle_hex8 import LAM as lam, MU as mu, _kelvin_grad2
+    D = 16000.0
+    sd, cd = np.sin(np.radians(dip)), np.cos(np.radians(dip))
+    s_, d_ = np.array([1.0, 0.0, 0.0]), np.array([0.0, cd, sd])
+    n_ = np.cross(s_, d_)
+    al1, al2, aw1, aw2 = -1.0, 1.0, -0.8, 0.7
+    g, w = np.polynomial.legendre.leggauss(12)
+
+    def nodes(a, c, npan=16):
+        e = np.linspace(a, c, npan + 1)
+        m, h = (e[:-1] + e[1:]) / 2, (e[1:] - e[:-1]) / 2
+        return (m[:, None] + h[:, None] * g[None, :]).ravel(), (h[:, None] * w[None, :]).ravel()
+
+    (XI, WXI), (ET, WET) = nodes(al1, al2), nodes(aw1, aw2)
+    P = (XI[:, None, None] * s_ + ET[None, :, None] * d_ + np.array([0.0, 0.0, -D])).reshape(-1, 3)
+    Wt = (WXI[:, None] * WET[None, :]).ravel()
+    x = np.array([r[0], r[1], r[2] - D])
+    G2w = np.einsum("nijkl,n->ijkl", _kelvin_grad2(x[None, :] - P), Wt)
+    alpha = (lam + mu) / (lam + 2 * mu)
+    for U in np.eye(3):
+        u, rc = oracle.dc3d(*x, alpha, D, dip, al1, al2, aw1, aw2, *U)
+        assert rc == 0
+        G = np.array([[u[3 + 3 * j + i] for j in range(3)] for i in range(3)])
+        b = U[0] * s_ + U[1] * d_ + U[2] * n_
+        eps = 0.5 * (np.outer(b, n_) + np.outer(n_, b))
+        m = lam * np.trace(eps) * np.eye(3) + 2 * mu * eps
+        K = -np.einsum("jk,ijkl->il", m, G2w)
+        assert np.abs(G - K).max() <= 1e-11 * np.abs(G).max()
