@@ -1,7 +1,7 @@
-"""The sweep's fault rows on the tensor cores (gbc_sweep_set_fault_product): against the SIMT engine's
-FP32 Toeplitz rows and over an integration window against single models. pytest does not collect
-this file (its name does not start with test_): the optional product segment it checks has not run
-on a GPU; it becomes test_gpu_sweep_fault_product.py once it has."""
+"""The sweep's fault rows on the tensor cores (gbc_sweep_set_fault_product): the dense fault-fault
+block as exact hi/mid/lo BF16 planes in the tcgen05 product, against the SIMT engine's FP32
+Toeplitz rows (K = 1, 5, 20: the 3 x 16 and 3 x 32-column instantiations) and over a one-year
+VCABM5 window against single models."""
 import numpy as np
 import pytest
 
