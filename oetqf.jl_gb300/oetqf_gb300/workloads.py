@@ -136,15 +136,28 @@ def fault_ensemble(n_models=256, years=50.0, seed=3, n_range=(200, 2000), nxi=10
 
 
 def serving_requests(n_requests=32, seed=5, mantle_fraction=0.25, patch_range=(500, 4096), cell_range=(0, 4000),
-                     year_range=(10.0, 200.0)) -> list[CycleModel]:
+                     year_range=(10.0, 200.0), geometries=None) -> list[CycleModel]:
+    """With geometries = G, every request takes one of G seeded (patch count, mantle size) shapes,
+    so requests repeat meshes (the case the server's Green's-function cache serves) while each
+    draws its own friction, initial state and horizon."""
     rng = SplitMix64(seed)
+    pool = None
+    if geometries:
+        pool = [(patch_range[0] + (patch_range[1] - patch_range[0]) * rng.uniform(1)[0],
+                 rng.uniform(1)[0] < mantle_fraction,
+                 max(1, int(cell_range[0] + (cell_range[1] - cell_range[0]) * rng.uniform(1)[0])))
+                for _ in range(int(geometries))]
     out = []
     for r in range(n_requests):
-        N = patch_range[0] + (patch_range[1] - patch_range[0]) * rng.uniform(1)[0]
+        if pool is not None:
+            N, with_mantle, ne_pick = pool[int(rng.uniform(1)[0] * len(pool)) % len(pool)]
+        else:
+            N = patch_range[0] + (patch_range[1] - patch_range[0]) * rng.uniform(1)[0]
         years = year_range[0] + (year_range[1] - year_range[0]) * rng.uniform(1)[0]
         member = fault_ensemble(n_models=1, years=years, seed=int(rng.next_u64() % 1000003), n_range=(N, N))[0]
-        if rng.uniform(1)[0] < mantle_fraction:
-            ne_target = max(1, int(cell_range[0] + (cell_range[1] - cell_range[0]) * rng.uniform(1)[0]))
+        if (with_mantle if pool is not None else rng.uniform(1)[0] < mantle_fraction):
+            ne_target = ne_pick if pool is not None else \
+                max(1, int(cell_range[0] + (cell_range[1] - cell_range[0]) * rng.uniform(1)[0]))
             nz = 4
             nxy = max(1, int(round((ne_target / nz) ** 0.5)))
             L = member.mf.nx * 1e3
