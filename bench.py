@@ -1,20 +1,23 @@
-"""Benchmark: simulated years per second of an earthquake-cycle model on one GB300.
+"""Benchmark: simulated years per second of earthquake-cycle models on one GB300.
 
-Workload (default): a 100 km x 10 km vertical strike-slip fault at 1 km cells (1000 patches) over a
-Maxwell mantle from 10 to 30 km depth (50 x 10 x 5 = 2500 cells), FP64 Green's functions and
-arithmetic, integrated for 100 simulated years with Tsit5 (reltol 1e-6, abstol 1e-8, dt0 1e-8 s,
-dtmax 0.2 yr). Synthetic seeded inputs (splitmix64); the Green's functions are assembled on the
-device before timing.
+Default line (the headline metric, batched mixed precision against the plain FP64 GPU path): 256
+independent fault-only models (patch counts U[200, 2000], per-model a - b, Dc, sigma; seeded
+splitmix64 synthetic inputs) integrated together by the persistent ensemble kernel (FP32 FFT
+convolution in shared memory, FP64 friction, theta state, stages and error norm; VCABM5 with the
+reference example's settings) over a fixed window of the horizon, as one batched call (the models
+never wait for each other); `ms_per_step` is that time divided by --steps. Warm-up integrates W
+short windows (0.01 yr) untimed. `value` keeps the state in HBM (gbc_ensemble_integrate_dev);
+`e2e` repeats the window through the host-buffer call gbc_ensemble_integrate (pinned host state in,
+final state out). The same line measures the plain FP64 GPU path on every one of the 256 models
+over the same window (each model alone through gbc_integrate, one after another), the slip-rate
+differences between the arms and the FP64 oracle, and, as sub-objects, the FP64 and 16-bit
+mantle GEMVs against their rooflines (the FP64 pipe peak is measured in the same run), the
+tensor-core sweep and a serving stream. Other workloads: --workload.
 
-A bench "step" is one window of the horizon (horizon / K): warm-up integrates W short windows
-(0.01 yr each, from the initial state) untimed; the timed region integrates the K windows that
-cover the whole horizon. `value` keeps the state in HBM (gbc_integrate_dev); `e2e` repeats the
-horizon through the host-buffer C-ABI call gbc_integrate (state copied host->device and back every
-window). The RHS is read-bound on 2.04 GB of Green's functions, far above the 129 MB L2.
-
---impl reference times the CPU oracle (the reference's algorithm restated in C with OpenMP; the
-Julia reference cannot run here) on the host cores. Under torchrun each rank integrates an
-independent replica (the path does not shard).
+--impl reference integrates the same 256 models over the same window on the host cores with the
+C/OpenMP FP64 oracle (the reference's algorithm restated in C, its FFT convolution through radix-2
+transforms; one model per host thread). Under torchrun each rank integrates an independent
+replica (the path does not shard).
 """
 from __future__ import annotations
 
@@ -44,10 +47,15 @@ RHS_FOR_HORIZON = {("fault-mantle-1000x2500-f64", "Tsit5"): 6 * 42388 + 1,
                    ("fault-mantle-1000x2500-f64", "VCABM5"): 138710,
                    ("fault-800-f64", "Tsit5"): 28543, ("fault-800-f64", "VCABM5"): 12381}
 WORKLOADS = ["fault-mantle-1000x2500-f64", "fault-800-f64"]
-# DRAM bytes (read + write) of one k_rows launch from ncu, per workload
-# (profiles/k_rows_fault-mantle-1000x2500-f64.md)
+# DRAM bytes (read + write) of one launch of the dominant kernel, read from an ncu capture of the
+# same workload (dram__bytes_read.sum + dram__bytes_write.sum); reported as `traffic` with its
+# source, since a live bench run cannot read hardware counters
 NCU_TRAFFIC = {"fault-mantle-1000x2500-f64": 2044237000 + 2987264,
                "fault-mantle-1000x2500-f64-df64": 2081574000 + 3372032}
+# the headline ensemble: window of the horizon integrated by every arm (all 256 models)
+ENSEMBLE_WINDOW_YR = 8.0
+# the loading phase before the ensemble's first events (the earliest starts after 3 years)
+SHORT_HORIZON_YR = 3.0
 
 
 def workload(name):
@@ -313,12 +321,8 @@ def run_gpu(args):
     r1.record(stream)
     r1.synchronize()
     rhs_ms = r0.elapsed_time(r1) / R
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
+    pk, psrc = peaks()
+    peak = pk["hbm_gbs"]
     achieved = rhs_bytes(cm) / (rhs_ms / 1e3) / 1e9
     traffic = NCU_TRAFFIC.get(args.workload + ("-df64" if args.storage == "df64" else ""))
     df64_line = None
@@ -382,7 +386,8 @@ def run_gpu(args):
                          "traffic": traffic, "rhs_ms": rhs_ms,
                          "kernel": "k_prologue + k_rows (one RHS)" if args.storage == "f64" else
                          "k_prologue_mixed + k_gemv_df64 (one RHS)",
-                         "bytes_per_launch": rhs_bytes(cm), "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"},
+                         "bytes_per_launch": rhs_bytes(cm), "peak_source": psrc,
+                         "traffic_source": "ncu capture of this workload"},
             "e2e": {"value": sim_yr / (e2e_ms / 1e3), "unit": "sim-yr/s", "h2d_bytes_per_step": int(cm.u0.nbytes),
                     "d2h_bytes_per_step": int(cm.u0.nbytes)},
             "clocks": clk, "gpu_launches": launches}
@@ -395,19 +400,11 @@ def run_gpu(args):
         line["cpu_baseline"], (pack, how, total_rhs) = cpu_oracle_sample(cm, args.workload, args.alg, gfs=gfs,
                                                                          budget_s=args.cpu_budget, nrhs_horizon=nrhs)
         line["cpu_baseline_twin"] = cpu_twin_sample(cm, pack, how, total_rhs)
-    if not args.no_sweep and ws == 1:
-        try:  # the tensor-core form: property variants sharing one geometry's Green's functions
-            line["sweep"] = sweep_summary(args)
-        except Exception as exc:
-            line["sweep"] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
     print(json.dumps(line), flush=True)
 
 
 def _peak():
-    try:
-        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
-    except Exception:
-        return 6800.0
+    return peaks()[0]["hbm_gbs"]
 
 
 def _base_line(metric_value, args, n_gpus, extra_cfg, ms, dtype):
@@ -433,7 +430,7 @@ def run_mixed_large(args):
     mode = C.GBC_PREC_BF16 if args.precision == "bf16" else C.GBC_PREC_F16
     N, E = cm.N, 6 * cm.ne
     out = {}
-    # the 16-bit arm integrates ln θ under Tsit5; VCABM5 integrates θ itself (see run_ensemble)
+    # the 16-bit arm integrates ln θ under Tsit5; VCABM5 integrates θ itself (as the ensemble does)
     mixed_lt = args.alg != "VCABM5"
     for name, md, lt in (("f64", C.GBC_PREC_F64, False), ("df64", C.GBC_PREC_DF64, False), (args.precision, mode, mixed_lt)):
         m.set_precision(md)
@@ -491,7 +488,7 @@ SWEEP_GEOMETRY = {"sweep-4096x8000": large_fault_with_mantle, "sweep-1000x2500":
 
 
 def sweep_measure(K, engine, years, steps, alg, warmup=3, fault_product=False, geometry="sweep-4096x8000",
-                  profile_rhs=0):
+                  profile_rhs=0, base=None):
     """Property variants of a viscoelastic model sharing its block-scaled BF16 Green's functions
     (gbc_sweep) over a window, and the single-model BF16 path on variant 0 over the same window in
     the same run. Returns the measurements (times from CUDA events on the sweep's and the model's
@@ -501,12 +498,15 @@ def sweep_measure(K, engine, years, steps, alg, warmup=3, fault_product=False, g
     from oetqf_gb300.equation import GB300Model
     from oetqf_gb300.property import PowerLawViscosityProperty, RateStateQuasiDynamicProperty
     from oetqf_gb300.sweep import Sweep
-    cm = SWEEP_GEOMETRY[geometry]()
-    m = GB300Model(cm.mf.nx, cm.mf.nξ, cm.ne)
-    m.assemble_gf(cm.mf, cm.ma, cm.lam, cm.mu)
-    m.set_fault_props(cm.pf)
-    m.set_mantle_props(cm.pa)
-    m.set_precision(C.GBC_PREC_BF16)
+    if base is not None:  # an assembled BF16 model of the same geometry (kept open for the caller)
+        m, cm = base
+    else:
+        cm = SWEEP_GEOMETRY[geometry]()
+        m = GB300Model(cm.mf.nx, cm.mf.nξ, cm.ne)
+        m.assemble_gf(cm.mf, cm.ma, cm.lam, cm.mu)
+        m.set_fault_props(cm.pf)
+        m.set_mantle_props(cm.pa)
+        m.set_precision(C.GBC_PREC_BF16)
     N, E = cm.N, 6 * cm.ne
     props, u0s = [], []
     for k in range(K):  # normal stress, state distance and mantle viscosity vary across the variants
@@ -533,7 +533,8 @@ def sweep_measure(K, engine, years, steps, alg, warmup=3, fault_product=False, g
         torch.cuda.synchronize()
         err = sw.error_word()
         sw.close()
-        m.close()
+        if base is None:
+            m.close()
         return {"profile_rhs": profile_rhs, "error_word": err}
     for _ in range(max(warmup, 3)):
         sw.rhs_dev(U.data_ptr(), DU.data_ptr())
@@ -573,24 +574,11 @@ def sweep_measure(K, engine, years, steps, alg, warmup=3, fault_product=False, g
         matrix_bytes += 6 * ((N + 127) // 128 * 128) ** 2
     reads = 1 if engine == "umma" else (K + 7) // 8
     sw.close()
-    m.close()
+    if base is None:
+        m.close()
     return {"value": K * years / (ms / 1e3), "ms": ms, "rhs_ms": rhs_ms, "single_value": years / (ms1 / 1e3),
             "rk_steps": [int(x) for x in rk], "err": float(np.abs(v_sw - v_1).max() / np.abs(v_1).max()),
             "bytes": matrix_bytes * reads, "N": N, "ne": cm.ne}
-
-
-def sweep_summary(args):
-    """The shared-geometry sweep on the tensor cores, 32 variants of the 4096 + 8000 model over one
-    20-year window, for the default bench line."""
-    r = sweep_measure(32, "umma", 20.0, 1, args.alg)
-    peak = _peak()
-    ach = r["bytes"] / (r["rhs_ms"] / 1e3) / 1e9
-    return {"workload": "sweep-4096x8000-bf16-K32", "variants": 32, "engine": "tcgen05", "window_yr": 20.0,
-            "value": r["value"], "unit": "sim-yr/s (all variants)", "single_model_bf16": r["single_value"],
-            "speedup_vs_single_model": r["value"] / r["single_value"],
-            "rhs_ms_all_variants": r["rhs_ms"], "rhs_roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak},
-            "rk_steps_per_variant_min_max": [min(r["rk_steps"]), max(r["rk_steps"])],
-            "variant0_max_slip_rate_rel_diff_vs_single_model": r["err"]}
 
 
 def run_sweep(args):
@@ -620,90 +608,6 @@ def run_sweep(args):
     line["single_model"] = {"value": r["single_value"], "unit": "sim-yr/s"}
     line["speedup_vs_single_model"] = line["value"] / r["single_value"]
     line["variant0_max_slip_rate_rel_diff_vs_single_model"] = r["err"]
-    print(json.dumps(line), flush=True)
-
-
-def run_ensemble(args):
-    """256 fault-only models of uneven size in one persistent launch vs the plain FP64 GPU path."""
-    import torch
-    from oetqf_gb300.ensemble import Ensemble
-    from oetqf_gb300.equation import GB300Model
-    years = args.years or 50.0
-    models = fault_ensemble(n_models=256, years=years)
-    e = Ensemble([(mm.mf.nx, mm.mf.nξ) for mm in models])
-    for i, mm in enumerate(models):
-        e.assemble(i, mm.mf, mm.lam, mm.mu)
-        e.set_fault_props(i, mm.pf)
-    u0 = np.zeros(e.state_len)
-    for i, mm in enumerate(models):
-        u0[e.offsets[i]:e.offsets[i] + mm.u0.size] = mm.u0
-    alg = args.alg
-    # VCABM5 integrates θ itself (as the reference and the oracle do): with ln θ the multistep method
-    # lands a tolerance-sized distance (~1e-4 at reltol 1e-6) away from the θ solution
-    log_theta = alg != "VCABM5"
-    e.set_log_theta(log_theta)
-    best, tim = e.autotune(u0, steps=200, alg=alg, **SOLVER)
-    stream = torch.cuda.ExternalStream(e.stream)
-    for _ in range(args.warmup):
-        e.integrate(u0, 0.0, 0.01 * YEAR, alg=alg, **SOLVER)
-    u = torch.tensor(u0, device="cuda")
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    st = e.integrate_dev(u.data_ptr(), 0.0, years * YEAR, alg=alg, **SOLVER)
-    e1.record(stream)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1)
-    steps = np.array([s.naccept + s.nreject for s in st])
-    value = 256 * years / (ms / 1e3)
-    # e2e through the host-buffer call
-    t0 = time.perf_counter()
-    e.integrate(u0, 0.0, years * YEAR, alg=alg, **SOLVER)
-    e2e_s = time.perf_counter() - t0
-    # plain FP64 GPU path on a sample of members
-    idx = np.linspace(0, 255, args.fp64_sample).astype(int)
-    tot = 0.0
-    for i in idx:
-        mm = models[i]
-        g = GB300Model(mm.mf.nx, mm.mf.nξ, 0)
-        g.assemble_gf(mm.mf, None, mm.lam, mm.mu)
-        g.set_fault_props(mm.pf)
-        t0 = time.perf_counter()
-        g.integrate(mm.u0, 0.0, years * YEAR, alg=alg, **SOLVER)
-        tot += time.perf_counter() - t0
-    fp64_total = tot / len(idx) * 256
-    # error vs the FP64 oracle over 2 years on a few members
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    errs = []
-    short = fault_ensemble(n_models=256, years=2.0)
-    for i in idx[:4]:
-        mm = short[i]
-        es = Ensemble([(mm.mf.nx, mm.mf.nξ)])
-        es.assemble(0, mm.mf, mm.lam, mm.mu)
-        es.set_fault_props(0, mm.pf)
-        es.set_log_theta(log_theta)
-        ug, _ = es.integrate(mm.u0, 0.0, 2.0 * YEAR, alg=alg, **SOLVER)
-        gf = O.gf_ff(mm.mf, mm.lam, mm.mu, fourier=True)
-        uc, _ = O.OracleModel(gf, mm.pf).integrate(mm.u0, 0.0, 2.0 * YEAR, reltol=SOLVER["reltol"], abstol=SOLVER["abstol"], dt0=SOLVER["dt"], dtmax=SOLVER["dtmax"], alg=alg)
-        N = mm.N
-        errs.append(float(np.abs(ug[:N] - uc[:N]).max() / np.abs(uc[:N]).max()))
-    line = _base_line(value, args, 1, {"workload": "ensemble-256-fault-only", "models": 256, "patches_total": int(sum(mm.N for mm in models)),
-                                       "patch_range": [int(min(mm.N for mm in models)), int(max(mm.N for mm in models))],
-                                       "horizon_yr": years, "solver": alg, "cta_threads": best, "autotune_s": tim,
-                                       "rk_steps_min_mean_max": [int(steps.min()), float(steps.mean()), int(steps.max())],
-                                       "slowest_member_patches": int(models[int(np.argmax(steps))].N),
-                                       "precision": "FP32 rFFT convolution in shared memory; FP64 friction, " +
-                                                    ("ln-theta" if log_theta else "theta") +
-                                                    " state, stages, error norm (step-size gain factors in FP32)",
-                                       "regroup": "models still running move to 2/4/8-CTA clusters as others finish",
-                                       "l2": "state and spectra L2-resident (per-model working set)"}, ms, "f32+f64")
-    line["fp64_gpu"] = {"value": 256 * years / fp64_total, "sample": f"{len(idx)} members integrated one at a time with the FP64 single-model path ({alg}), scaled to 256"}
-    line["speedup_vs_fp64_gpu"] = value / line["fp64_gpu"]["value"]
-    line["max_slip_rate_rel_err_vs_fp64_oracle_2yr"] = max(errs)
-    line["e2e"] = {"value": 256 * years / e2e_s, "unit": "sim-yr/s", "h2d_bytes_per_step": int(u0.nbytes), "d2h_bytes_per_step": int(u0.nbytes)}
-    line["roofline"] = {"bound": "latency/fp64", "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None,
-                        "note": "per-model persistent CTAs; the makespan is set by the most eventful member"}
     print(json.dumps(line), flush=True)
 
 
@@ -744,26 +648,474 @@ def run_serving(args):
     print(json.dumps(line), flush=True)
 
 
+# ---- peaks ----------------------------------------------------------------------------------
+FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+
+
+def peaks():
+    """The machine's measured copy bandwidth and BF16 GEMM rate, else the stated fallback."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return {k: float(d[k]) for k in FALLBACK_PEAKS if k in d}, "measured (MEASURED_PEAKS.json)"
+    except Exception:
+        return dict(FALLBACK_PEAKS), "fallback (MEASURED_PEAKS.json absent: 6.8 TB/s, 1.9 PFLOP/s)"
+
+
+def fp64_fma_peak(torch, C, reps=3):
+    """FP64 FMA throughput of this GPU (FLOP/s), from gbc_probe_fp64_fma timed with CUDA events on
+    the stream it runs on: 8 CTAs of 256 threads per SM, 8 independent chains per thread."""
+    import ctypes
+    blocks = torch.cuda.get_device_properties(0).multi_processor_count * 8
+    out = torch.empty(blocks * 256, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream()
+    flops = ctypes.c_double()
+    h = ctypes.c_void_p(st.cuda_stream)
+    C.check(C.lib().gbc_probe_fp64_fma(ctypes.c_void_p(out.data_ptr()), blocks, 256, 512, h, ctypes.byref(flops)))
+    best = 0.0
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        C.check(C.lib().gbc_probe_fp64_fma(ctypes.c_void_p(out.data_ptr()), blocks, 256, 16384, h, ctypes.byref(flops)))
+        e1.record(st)
+        e1.synchronize()
+        best = max(best, flops.value / (e0.elapsed_time(e1) / 1e3))
+    return best
+
+
+# ---- the headline: 256-model ensemble vs the plain FP64 GPU path --------------------------------
+def ensemble_of(models):
+    from oetqf_gb300.ensemble import Ensemble
+    e = Ensemble([(mm.mf.nx, mm.mf.nξ) for mm in models])
+    for i, mm in enumerate(models):
+        e.assemble(i, mm.mf, mm.lam, mm.mu)
+        e.set_fault_props(i, mm.pf)
+    u0 = np.zeros(e.state_len)
+    for i, mm in enumerate(models):
+        u0[e.offsets[i]:e.offsets[i] + mm.u0.size] = mm.u0
+    return e, u0
+
+
+def fp64_arm(models, years, alg, torch):
+    """Every model alone through the plain FP64 single-model path (gbc_integrate_dev on its own
+    stream), one after another, over [0, years]; each call bracketed by CUDA events on the model's
+    stream (the host's graph capture and relaunch loop fall inside the bracket). Returns the total
+    milliseconds, per-model final states, step counts and statuses."""
+    from oetqf_gb300.equation import GB300Model
+    total_ms, finals, steps, status = 0.0, [], [], []
+    for mm in models:
+        g = GB300Model(mm.mf.nx, mm.mf.nξ, 0)
+        g.assemble_gf(mm.mf, None, mm.lam, mm.mu)
+        g.set_fault_props(mm.pf)
+        u = torch.tensor(mm.u0, device="cuda")
+        s = torch.cuda.ExternalStream(g.stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        st = g.integrate_dev(u.data_ptr(), 0.0, years * YEAR, alg=alg, **SOLVER)
+        e1.record(s)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        finals.append(u.cpu().numpy())
+        steps.append(int(st.naccept + st.nreject))
+        status.append(int(st.status))
+        g.close()
+    return total_ms, finals, steps, status
+
+
+def short_horizon_errors(models, u_short, offs, alg, torch):
+    """Slip rates of every model after the loading phase (SHORT_HORIZON_YR): the batched form and the
+    plain FP64 GPU path against the FP64 oracle (FFT convolution, all host threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    _, f_short, _, _ = fp64_arm(models, SHORT_HORIZON_YR, alg, torch)
+    oms = [O.OracleModel(O.gf_ff(mm.mf, mm.lam, mm.mu, fourier=True), mm.pf) for mm in models]
+    orc, st = O.integrate_many(oms, [mm.u0 for mm in models], 0.0, SHORT_HORIZON_YR * YEAR, reltol=SOLVER["reltol"],
+                               abstol=SOLVER["abstol"], dt0=SOLVER["dt"], dtmax=SOLVER["dtmax"], alg=alg, fft=True)
+    eb, ef = [], []
+    for i, mm in enumerate(models):
+        ref = orc[i][:mm.N]
+        eb.append(float(np.abs(u_short[offs[i]:offs[i] + mm.N] - ref).max() / np.abs(ref).max()))
+        ef.append(float(np.abs(f_short[i][:mm.N] - ref).max() / np.abs(ref).max()))
+    return {"at": f"{SHORT_HORIZON_YR:g} yr (the loading phase), every model, max |v - v_oracle| / max |v_oracle|",
+            "batched_vs_oracle": {"max": max(eb), "median": float(np.median(eb))},
+            "fp64_gpu_vs_oracle": {"max": max(ef), "median": float(np.median(ef))},
+            "oracle_failed": int(sum(1 for x in st if x.status != 0))}
+
+
+def run_headline(args):
+    import ctypes
+    import torch
+    from oetqf_gb300 import _capi as C
+
+    tdist, rank, ws = dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    years = args.years or ENSEMBLE_WINDOW_YR
+    alg = args.alg
+    models = fault_ensemble(n_models=256, years=years)
+    n = len(models)
+    t_asm = time.perf_counter()
+    e, u0 = ensemble_of(models)
+    t_asm = time.perf_counter() - t_asm
+    # VCABM5 integrates θ itself (as the reference and the oracle do); Tsit5 runs on ln θ
+    log_theta = alg != "VCABM5"
+    e.set_log_theta(log_theta)
+    best, tim = e.autotune(u0, steps=200, alg=alg, **SOLVER)
+    stream = torch.cuda.ExternalStream(e.stream)
+    for _ in range(args.warmup):
+        e.integrate(u0, 0.0, 0.01 * YEAR, alg=alg, **SOLVER)
+    K = args.steps
+    u = torch.tensor(u0, device="cuda")
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    if tdist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    launches0 = C.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    # the window as one batched call: every model runs at its own pace and none waits for another
+    # (K synchronised sub-windows would make the models meet at every edge, each sub-window lasting
+    # as long as its slowest model: 5x the time on this workload); K divides the timed region
+    st = e.integrate_dev(u.data_ptr(), 0.0, years * YEAR, alg=alg, **SOLVER)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    if tdist:
+        tdist.barrier()
+    ms = e0.elapsed_time(e1)
+    launches = C.kernel_launches() - launches0
+    clk = clocks.stop()
+    steps = np.array([x.naccept + x.nreject for x in st], dtype=np.int64)
+    rejects = np.array([x.nreject for x in st], dtype=np.int64)
+    bad = [i for i, x in enumerate(st) if x.status != 0]
+    if bad:
+        raise SystemExit(f"ensemble members {bad[:8]} failed")
+    ms = max_over_ranks(tdist, ms, "cuda")
+    value = replica_throughput(ws, n * years, ms)
+    u_ens = u.cpu().numpy()
+    # e2e: the same window through the host-buffer call (pinned host state in, final state out)
+    uh = torch.tensor(u0).pin_memory()
+    un = uh.numpy()
+    o = e._opts(SOLVER["reltol"], SOLVER["abstol"], SOLVER["dt"], SOLVER["dtmax"], 10**9, alg)
+    torch.cuda.synchronize()
+    x0, x1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    x0.record(stream)
+    t0a, t1a = np.zeros(n), np.full(n, years * YEAR)
+    sts = (C.SolverStats * n)()
+    C.check(C.lib().gbc_ensemble_integrate(e.h, C.ptr(un), C.ptr(t0a), C.ptr(t1a), ctypes.byref(o), sts))
+    x1.record(stream)
+    x1.synchronize()
+    e2e_ms = x0.elapsed_time(x1)
+    e2e_same = bool(np.array_equal(un, u_ens))
+    offs = list(e.offsets)
+    # the loading phase before the first events (every model), for the short-horizon comparison
+    u_s = torch.tensor(u0, device="cuda")
+    e.integrate_dev(u_s.data_ptr(), 0.0, SHORT_HORIZON_YR * YEAR, alg=alg, **SOLVER)
+    u_short = u_s.cpu().numpy()
+    e.close()
+    if rank != 0:
+        return
+    line = {"metric": "sim-yr/s", "value": value, "unit": "sim-yr/s", "n_gpus": ws, "steps": K, "warmup": args.warmup,
+            "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64", "data": "synthetic (seeded splitmix64)"}
+    line["config"] = {"workload": "ensemble-256-fault-only", "models": n,
+                      "patches_total": int(sum(mm.N for mm in models)),
+                      "patch_range": [int(min(mm.N for mm in models)), int(max(mm.N for mm in models))],
+                      "window_yr": years,
+                      "steps": f"the window is integrated by one batched call; ms_per_step = that time / {K}",
+                      "solver": f"{alg} reltol 1e-6 abstol 1e-8 dt0 1e-8 s dtmax 0.2 yr (examples/otf-with-mantle.jl:160-162)",
+                      "precision": "FP32 rFFT convolution in shared memory; FP64 friction, " +
+                                   ("ln-theta" if log_theta else "theta") + " state, stages, error norm",
+                      "cta_threads": best, "assembly_s": round(t_asm, 2),
+                      "rk_steps_min_mean_max": [int(steps.min()), float(steps.mean()), int(steps.max())],
+                      "rk_rejected": int(rejects.sum()),
+                      "slowest_member": {"index": int(np.argmax(steps)), "patches": int(models[int(np.argmax(steps))].N),
+                                         "steps": int(steps.max()),
+                                         "us_per_step": ms * 1e3 / float(steps.max())},
+                      "l2": "per-model state and spectra are L2-resident (a few MB in all); no flush between steps",
+                      "parallelism": "replicas"}
+    line["e2e"] = {"value": ws * n * years / (e2e_ms / 1e3), "unit": "sim-yr/s",
+                   "h2d_bytes_per_step": int(u0.nbytes) // K, "d2h_bytes_per_step": int(u0.nbytes) // K,
+                   "call": "gbc_ensemble_integrate (pinned host state in, final state out: one call for the window)",
+                   "final_state_equals_device_run": e2e_same}
+    line["clocks"] = clk
+    line["gpu_launches"] = launches
+    # the plain FP64 GPU path on every model over the same window
+    f_ms, finals, f_steps, f_status = fp64_arm(models, years, alg, torch)
+    fp64_value = n * years / (f_ms / 1e3)
+    errs = np.array([float(np.abs(u_ens[offs[i]:offs[i] + mm.N] - finals[i][:mm.N]).max() /
+                           np.abs(finals[i][:mm.N]).max()) for i, mm in enumerate(models)])
+    line["fp64_gpu"] = {"value": fp64_value, "unit": "sim-yr/s", "ms": f_ms, "models": n, "window_yr": years,
+                        "how": "each model alone through the plain FP64 single-model path (gbc_integrate_dev: FP64 "
+                               "Toeplitz rows, FP64 friction, the same VCABM5), one after another, CUDA events around "
+                               "each call",
+                        "rk_steps_total": int(sum(f_steps)), "failed": int(sum(1 for x in f_status if x != 0))}
+    line["speedup_vs_fp64_gpu"] = value / fp64_value
+    line["slip_rate_rel_diff_vs_fp64_gpu"] = {
+        "at": f"window end ({years:g} yr), every model: max |v_batched - v_fp64| / max |v_fp64| (after the first "
+              f"events the cycles are chaotic: any rounding difference grows, for the FP64 path as well, see "
+              f"slip_rate_rel_diff_vs_fp64_oracle)",
+        "max": float(errs.max()), "median": float(np.median(errs)), "p90": float(np.percentile(errs, 90)),
+        "models_within_1e-4": int((errs <= 1e-4).sum())}
+    line["slip_rate_rel_diff_short_horizon"] = short_horizon_errors(models, u_short, offs, alg, torch)
+    pk, psrc = peaks()
+    fpk = fp64_fma_peak(torch, C)
+    line["fp64_peak"] = {"value": fpk / 1e12, "unit": "TFLOP/s", "how": "gbc_probe_fp64_fma, CUDA events, this run"}
+    if not args.no_sub and ws == 1:
+        # the matvec kernels against their bounds, measured in the same run
+        try:
+            line["fault_mantle_1000x2500"] = sub_fault_mantle_f64(torch, C, fpk, pk, psrc)
+        except Exception as exc:
+            line["fault_mantle_1000x2500"] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
+        try:
+            line["fault_mantle_4096x8000"] = sub_mixed_4096(torch, C, pk, psrc, alg, sweep=not args.no_sweep)
+        except Exception as exc:
+            line["fault_mantle_4096x8000"] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
+        mx = line.get("fault_mantle_4096x8000", {}).get("bf16")
+        if mx:
+            line["roofline"] = {"bound": "hbm", "achieved": mx["achieved"], "peak": mx["peak"], "unit": "GB/s",
+                                "frac": mx["frac"], "traffic": None, "kernel": mx["kernel"], "rhs_ms": mx["rhs_ms"],
+                                "bytes_per_launch": mx["bytes_per_rhs"], "peak_source": psrc,
+                                "note": "the 16-bit mantle GEMV of the mixed-precision form; the ensemble kernel "
+                                        "itself is bound by the latency of its dependent phases (its spectra and "
+                                        "state stay in shared memory and L2), so no HBM or tensor roofline applies to it"}
+    if not args.no_serving and ws == 1:
+        try:
+            line["serving"] = sub_serving(args)
+        except Exception as exc:
+            line["serving"] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
+    if not args.no_cpu and ws == 1:
+        cb, done = cpu_ensemble_sample(models, years, alg)
+        line["cpu_baseline"] = cb
+        oe, of = [], []
+        for i, uo in done.items():
+            if uo is None:
+                continue
+            mm = models[i]
+            ref = uo[:mm.N]
+            oe.append(float(np.abs(u_ens[offs[i]:offs[i] + mm.N] - ref).max() / np.abs(ref).max()))
+            of.append(float(np.abs(finals[i][:mm.N] - ref).max() / np.abs(ref).max()))
+        if oe:
+            line["slip_rate_rel_diff_vs_fp64_oracle"] = {
+                "at": f"window end ({years:g} yr), the sampled models that reached it on the oracle",
+                "models": len(oe), "batched": {"max": max(oe), "median": float(np.median(oe))},
+                "fp64_gpu": {"max": max(of), "median": float(np.median(of))}}
+    print(json.dumps(line), flush=True)
+
+
+def sub_fault_mantle_f64(torch, C, fp64_peak, pk, psrc):
+    """The 1000-patch + 2500-cell model (FP64 Green's functions, 2.04 GB read per RHS): the FP64 row
+    GEMV (k_prologue + k_rows) against the measured FP64 FMA peak and against HBM, and the FP64-accurate
+    double-float GEMV (k_gemv_df64) against HBM; CUDA events on the model's stream, 30 RHS each."""
+    from oetqf_gb300.equation import GB300Model
+    cm = strike_slip_with_mantle()
+    m = GB300Model(cm.mf.nx, cm.mf.nξ, cm.ne)
+    t = time.perf_counter()
+    m.assemble_gf(cm.mf, cm.ma, cm.lam, cm.mu)
+    t = time.perf_counter() - t
+    m.set_fault_props(cm.pf)
+    m.set_mantle_props(cm.pa)
+    stream = torch.cuda.ExternalStream(m.stream)
+    u = torch.tensor(cm.u0, device="cuda")
+    du = torch.zeros_like(u)
+
+    def rhs_ms(R=30):
+        for _ in range(3):
+            m.rhs_dev(u.data_ptr(), du.data_ptr())
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        r0.record(stream)
+        for _ in range(R):
+            m.rhs_dev(u.data_ptr(), du.data_ptr())
+        r1.record(stream)
+        r1.synchronize()
+        return r0.elapsed_time(r1) / R
+
+    N, E = cm.N, 6 * cm.ne
+    entries = E * (N + E) + N * E + N * N   # mantle rows, mantle->fault rows, Toeplitz sum (one FMA each)
+    f64 = rhs_ms()
+    m.set_precision(C.GBC_PREC_DF64)
+    df = rhs_ms()
+    m.close()
+    b = rhs_bytes(cm)
+    ach, achd = b / (f64 / 1e3) / 1e9, b / (df / 1e3) / 1e9
+    flops = 2.0 * entries / (f64 / 1e3)
+    return {"workload": "fault-mantle-1000x2500-f64", "assembly_s": round(t, 2), "bytes_per_rhs": b,
+            "f64": {"kernel": "k_prologue + k_rows (one RHS)", "rhs_ms": f64, "bound": "fp64",
+                    "achieved_tflops": flops / 1e12, "peak_tflops": fp64_peak / 1e12, "frac": flops / fp64_peak,
+                    "peak_source": "measured in this run (gbc_probe_fp64_fma, CUDA events)",
+                    "hbm": {"achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": ach / pk["hbm_gbs"],
+                            "peak_source": psrc},
+                    "traffic": NCU_TRAFFIC["fault-mantle-1000x2500-f64"], "traffic_source": "ncu capture of this workload"},
+            "df64": {"kernel": "k_prologue_mixed + k_gemv_df64 (one RHS)", "rhs_ms": df, "bound": "hbm", "achieved": achd,
+                     "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achd / pk["hbm_gbs"], "peak_source": psrc,
+                     "traffic": NCU_TRAFFIC["fault-mantle-1000x2500-f64-df64"],
+                     "traffic_source": "ncu capture of this workload"}}
+
+
+def sub_mixed_4096(torch, C, pk, psrc, alg, sweep=True):
+    """The 4096-patch + 8000-cell model: the block-scaled BF16 GEMV (k_gemv_tma, 5.394 GB per RHS)
+    against HBM, and on the same assembled Green's functions the 32-variant tensor-core sweep
+    (k_sw_gemm_umma, fault rows on the tensor cores too) over a 20-year window against the
+    single-model BF16 path."""
+    from oetqf_gb300.equation import GB300Model
+    cm = large_fault_with_mantle()
+    m = GB300Model(cm.mf.nx, cm.mf.nξ, cm.ne)
+    t = time.perf_counter()
+    m.assemble_gf(cm.mf, cm.ma, cm.lam, cm.mu)
+    t = time.perf_counter() - t
+    m.set_fault_props(cm.pf)
+    m.set_mantle_props(cm.pa)
+    m.set_precision(C.GBC_PREC_BF16)
+    stream = torch.cuda.ExternalStream(m.stream)
+    u = torch.tensor(cm.u0, device="cuda")
+    du = torch.zeros_like(u)
+    for _ in range(3):
+        m.rhs_dev(u.data_ptr(), du.data_ptr())
+    r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    r0.record(stream)
+    for _ in range(20):
+        m.rhs_dev(u.data_ptr(), du.data_ptr())
+    r1.record(stream)
+    r1.synchronize()
+    rms = r0.elapsed_time(r1) / 20
+    N, E = cm.N, 6 * cm.ne
+    b = (E * (N + E) + N * E) * 2
+    ach = b / (rms / 1e3) / 1e9
+    out = {"workload": "fault-mantle-4096x8000-bf16", "assembly_s": round(t, 2),
+           "bf16": {"kernel": "k_prologue_mixed + k_gemv_tma + k_fault_rows_smem (one RHS)", "rhs_ms": rms,
+                    "bytes_per_rhs": b, "bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                    "frac": ach / pk["hbm_gbs"], "peak_source": psrc}}
+    if sweep:
+        try:
+            r = sweep_measure(32, "umma", 20.0, 1, alg, fault_product=True, base=(m, cm))
+            ach = r["bytes"] / (r["rhs_ms"] / 1e3) / 1e9
+            out["sweep"] = {"workload": "sweep-4096x8000-bf16-K32", "variants": 32, "engine": "tcgen05",
+                            "fault_rows": "tensor-core product (exact hi/mid/lo BF16 planes)", "window_yr": 20.0,
+                            "value": r["value"], "unit": "sim-yr/s (all variants)", "single_model_bf16": r["single_value"],
+                            "speedup_vs_single_model": r["value"] / r["single_value"],
+                            "rhs_ms_all_variants": r["rhs_ms"],
+                            "rhs_roofline": {"achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                                             "frac": ach / pk["hbm_gbs"], "peak_source": psrc,
+                                             "bytes": r["bytes"]},
+                            "rk_steps_per_variant_min_max": [min(r["rk_steps"]), max(r["rk_steps"])],
+                            "variant0_max_slip_rate_rel_diff_vs_single_model": r["err"]}
+        except Exception as exc:
+            out["sweep"] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
+    m.close()
+    return out
+
+
+def cpu_ensemble_sample(models, years, alg, budget_steps=40000, every=16):
+    """A bounded sample of the ensemble workload on the host cores: every `every`-th model over the
+    same window with the C/OpenMP FP64 oracle (FFT convolution, one model per host thread), each
+    capped at budget_steps steps. Returns (cpu_baseline dict, {model index: final state or None})."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    idx = list(range(0, len(models), every))
+    oms = [O.OracleModel(O.gf_ff(models[i].mf, models[i].lam, models[i].mu, fourier=True), models[i].pf) for i in idx]
+    t0 = time.perf_counter()
+    finals, st = O.integrate_many(oms, [models[i].u0 for i in idx], 0.0, years * YEAR, reltol=SOLVER["reltol"],
+                                  abstol=SOLVER["abstol"], dt0=SOLVER["dt"], dtmax=SOLVER["dtmax"], alg=alg,
+                                  maxiters=budget_steps, fft=True)
+    wall = time.perf_counter() - t0
+    sim = sum(s.t for s in st) / YEAR
+    done = {i: (f if s.status == 0 else None) for i, f, s in zip(idx, finals, st)}
+    cores = O.num_threads()
+    return ({"value": sim / wall, "unit": "sim-yr/s", "cores": cores, "kind": "port",
+             "sample": f"{len(idx)} of the 256 models (every {every}th) over the same {years:g}-yr window on the "
+                       f"C/OpenMP FP64 oracle (FFT convolution, one model per host thread, {alg}), each capped at "
+                       f"{budget_steps} steps: {sum(1 for s in st if s.status == 0)} reached the window end, "
+                       f"{sim:.2f} sim-yr in {wall:.1f} s"}, done)
+
+
+def sub_serving(args, n_requests=200):
+    """A Poisson stream (20 requests/s) of fault and fault+mantle requests drawn from 8 geometries
+    (so the Green's-function cache is exercised), horizons of 1 to 10 years."""
+    from oetqf_gb300.serving import Server, run_stream
+    reqs = serving_requests(n_requests=n_requests, geometries=8, year_range=(1.0, 10.0))
+    s = Server(hbm_budget_gb=args.hbm_budget_gb, alg=args.alg)
+    out = run_stream(s, reqs, rate_per_s=20.0, seed=1)
+    info = s.info()
+    s.close()
+    lat = out["latency_s"]
+    return {"workload": "serving-poisson-20rps-8-geometries", "requests": len(reqs),
+            "mantle_requests": sum(r.ma is not None for r in reqs), "horizon_yr_range": [1.0, 10.0],
+            "value": out["sim_yr_per_s"], "unit": "sim-yr/s (aggregate)", "makespan_s": out["makespan_s"],
+            "latency_s": {"p50": out["p50_s"], "p99": out["p99_s"], "max": float(lat.max())},
+            "gf_cache": {"hits": info.cache_hits, "misses": info.cache_misses},
+            "peak_bytes": info.peak_bytes, "batch_iterations": info.iterations, "status": out["status"]}
+
+
+def run_reference_ensemble(args):
+    """The reference arm of the headline: the same 256 models over the same window on the host cores
+    with the C/OpenMP FP64 oracle (the reference's ode and integrator restated in C; its traction-rate
+    convolution through radix-2 FFTs, as the reference applies it through FFTW; one model per host
+    thread, each thread taking the next model when done). Measured end to end, nothing scaled."""
+    tdist, rank, ws = dist()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    years = args.years or ENSEMBLE_WINDOW_YR
+    alg = args.alg
+    models = fault_ensemble(n_models=256, years=years)
+    n = len(models)
+    oms = [O.OracleModel(O.gf_ff(mm.mf, mm.lam, mm.mu, fourier=True), mm.pf) for mm in models]
+    S = dict(reltol=SOLVER["reltol"], abstol=SOLVER["abstol"], dt0=SOLVER["dt"], dtmax=SOLVER["dtmax"], alg=alg, fft=True)
+    for _ in range(args.warmup):
+        O.integrate_many(oms, [mm.u0 for mm in models], 0.0, 0.01 * YEAR, **S)
+    K = args.steps
+    t0 = time.perf_counter()
+    states, st = O.integrate_many(oms, [mm.u0 for mm in models], 0.0, years * YEAR, **S)
+    wall = time.perf_counter() - t0
+    steps = sum(s.naccept + s.nreject for s in st)
+    bad = [i for i, s in enumerate(st) if s.status != 0]
+    if bad:
+        raise SystemExit(f"oracle models {bad[:8]} failed")
+    v = n * years / wall
+    cores = O.num_threads()
+    line = {"metric": "sim-yr/s", "value": v, "unit": "sim-yr/s", "n_gpus": ws, "steps": K, "warmup": args.warmup,
+            "ms_per_step": wall * 1e3 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded splitmix64)", "impl": "reference",
+            "config": {"workload": "ensemble-256-fault-only", "models": n,
+                       "patches_total": int(sum(mm.N for mm in models)),
+                       "patch_range": [int(min(mm.N for mm in models)), int(max(mm.N for mm in models))],
+                       "window_yr": years,
+                       "steps": f"the window is integrated by one batched call; ms_per_step = that time / {K}",
+                       "solver": f"{alg} reltol 1e-6 abstol 1e-8 dt0 1e-8 s dtmax 0.2 yr (examples/otf-with-mantle.jl:160-162)",
+                       "precision": "f64"},
+            "cpu_baseline": {"value": v, "unit": "sim-yr/s", "cores": cores, "kind": "port",
+                             "sample": f"all {n} models over the whole {years:g}-yr window in one call on the "
+                                       f"C/OpenMP FP64 oracle ({alg}, FFT convolution, one model per host thread): "
+                                       f"{steps} steps in {wall:.1f} s, nothing scaled"},
+            "e2e": {"value": v, "unit": "sim-yr/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbcycle", choices=["gbcycle", "reference"])
-    ap.add_argument("--workload", default="fault-mantle-1000x2500-f64",
-                    choices=WORKLOADS + ["fault-mantle-4096x8000-mixed", "ensemble-256", "serving",
-                                                       "ensemble-profile", "sweep-4096x8000", "sweep-1000x2500"])
+    ap.add_argument("--workload", default="ensemble-256",
+                    choices=["ensemble-256"] + WORKLOADS + ["fault-mantle-4096x8000-mixed", "serving", "ensemble-profile",
+                                                           "sweep-4096x8000", "sweep-1000x2500"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "f16"])
     ap.add_argument("--alg", default=None, choices=["VCABM5", "Tsit5"],
                     help="integrator (default: VCABM5, the reference example's solver; with it the state holds θ; "
                          "Tsit5 runs the 16-bit and ensemble workloads on ln θ)")
-    ap.add_argument("--fp64-sample", type=int, default=8)
     ap.add_argument("--requests", type=int, default=32)
     ap.add_argument("--hbm-budget-gb", type=float, default=64.0)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-sub", action="store_true", help="default line: skip the GEMV / sweep sub-measurements")
+    ap.add_argument("--no-serving", action="store_true", help="default line: skip the serving-stream sub-measurement")
     ap.add_argument("--profile-rhs", type=int, default=0, help="run N right-hand sides only (for ncu captures)")
-    ap.add_argument("--years", type=float, default=0.0, help="override the horizon (profiling runs only)")
+    ap.add_argument("--years", type=float, default=0.0,
+                    help="override the window (default line: %g yr) or a workload's horizon" % ENSEMBLE_WINDOW_YR)
     ap.add_argument("--profile-precision", default="f64", choices=["f64", "bf16", "f16", "df64"])
     ap.add_argument("--variants", type=int, default=32, help="property variants of the sweep workload")
     ap.add_argument("--engine", default="umma", choices=["simt", "umma"], help="product engine of the sweep workload")
@@ -775,11 +1127,14 @@ def main():
     if args.alg is None:
         args.alg = "Tsit5" if args.workload == "ensemble-profile" else "VCABM5"
     if args.impl == "reference":
-        run_reference(args)
+        if args.workload == "ensemble-256":
+            run_reference_ensemble(args)
+        else:
+            run_reference(args)
     elif args.workload == "fault-mantle-4096x8000-mixed":
         run_mixed_large(args)
     elif args.workload == "ensemble-256":
-        run_ensemble(args)
+        run_headline(args)
     elif args.workload == "ensemble-profile":
         run_ensemble_profile(args)
     elif args.workload == "serving":
