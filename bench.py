@@ -1084,8 +1084,7 @@ def run_reference_ensemble(args):
                        "patch_range": [int(min(mm.N for mm in models)), int(max(mm.N for mm in models))],
                        "window_yr": years,
                        "steps": f"the window is integrated by one batched call; ms_per_step = that time / {K}",
-                       "solver": f"{alg} reltol 1e-6 abstol 1e-8 dt0 1e-8 s dtmax 0.2 yr (examples/otf-with-mantle.jl:160-162)",
-                       "precision": "f64"},
+                       "solver": f"{alg} reltol 1e-6 abstol 1e-8 dt0 1e-8 s dtmax 0.2 yr (examples/otf-with-mantle.jl:160-162)"},
             "cpu_baseline": {"value": v, "unit": "sim-yr/s", "cores": cores, "kind": "port",
                              "sample": f"all {n} models over the whole {years:g}-yr window in one call on the "
                                        f"C/OpenMP FP64 oracle ({alg}, FFT convolution, one model per host thread): "
