@@ -93,51 +93,85 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(
 // twiddles e^{-2πi t/P}, inverse their conjugates (no scaling). Two consecutive radix-2 stages are
 // done per pass with a thread's four elements in registers (the same operations in the same
 // order), so a pass needs one barrier instead of two.
+__device__ __forceinline__ float2 bfly_add(float2 a, float2 c) { return make_float2(a.x + c.x, a.y + c.y); }
+__device__ __forceinline__ float2 bfly_sub(float2 a, float2 c) { return make_float2(a.x - c.x, a.y - c.y); }
+__device__ __forceinline__ float2 tw_get(const float2* tw, int idx, int inverse) {
+    float2 w = tw[idx];
+    if (inverse) w.y = -w.y;
+    return w;
+}
+
+// in-place radix-2 DIT FFT of nq arrays of length P (P = 2^logP) already in bit-reversed order;
+// forward uses twiddles e^{-2πi t/P}, inverse their conjugates (no scaling). Up to three
+// consecutive radix-2 stages are done per pass with a thread's eight elements in registers (the
+// same butterflies in the same order as one stage per pass), so a 512-point transform takes three
+// passes and barriers; indices come from shifts (P is a power of two).
 template <int BS>
 __device__ __forceinline__ void fft_many(float2* Z, int nq, int P, int logP, const float2* tw, int inverse) {
     int st = 0;
     while (st < logP) {
-        if (st + 1 < logP) {
-            const int h = 1 << st;
-            const int quarter = P >> 2;
-            const int s1 = P / (2 * h), s2 = P / (4 * h);
-            for (int t = threadIdx.x; t < nq * quarter; t += BS) {
-                const int q = t / quarter, r = t - q * quarter;
-                const int g = r >> st, pos = r & (h - 1);
+        const int ns = min(3, logP - st);       // stages in this pass
+        const int h = 1 << st;
+        const int lgi = logP - ns;              // log2 of the butterfly groups per array
+        const int items = nq << lgi;
+        for (int t = threadIdx.x; t < items; t += BS) {
+            const int q = t >> lgi, r = t & ((1 << lgi) - 1);
+            const int g = r >> st, pos = r & (h - 1);
+            float2* z = Z + (size_t)q * P;
+            if (ns == 3) {
+                const int b0 = g * 8 * h + pos;
+                float2 x[8];
+#pragma unroll
+                for (int m = 0; m < 8; ++m) x[m] = z[b0 + m * h];
+                const float2 w1 = tw_get(tw, pos * (P >> (st + 1)), inverse);
+#pragma unroll
+                for (int m = 0; m < 8; m += 2) {  // stage st: pairs (m, m+1)
+                    const float2 c = cmul(x[m + 1], w1);
+                    x[m + 1] = bfly_sub(x[m], c);
+                    x[m] = bfly_add(x[m], c);
+                }
+#pragma unroll
+                for (int m = 0; m < 8; ++m) {     // stage st+1: pairs (m, m+2) in groups of four
+                    if (m & 2) continue;
+                    const float2 w = tw_get(tw, (pos + (m & 1) * h) * (P >> (st + 2)), inverse);
+                    const float2 c = cmul(x[m + 2], w);
+                    x[m + 2] = bfly_sub(x[m], c);
+                    x[m] = bfly_add(x[m], c);
+                }
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {     // stage st+2: pairs (m, m+4)
+                    const float2 w = tw_get(tw, (pos + m * h) * (P >> (st + 3)), inverse);
+                    const float2 c = cmul(x[m + 4], w);
+                    x[m + 4] = bfly_sub(x[m], c);
+                    x[m] = bfly_add(x[m], c);
+                }
+#pragma unroll
+                for (int m = 0; m < 8; ++m) z[b0 + m * h] = x[m];
+            } else if (ns == 2) {
                 const int b0 = g * 4 * h + pos;
-                float2* z = Z + q * P;
-                float2 w1 = tw[pos * s1], w2a = tw[pos * s2], w2b = tw[(pos + h) * s2];
-                if (inverse) { w1.y = -w1.y; w2a.y = -w2a.y; w2b.y = -w2b.y; }
-                float2 x0 = z[b0], x1 = z[b0 + h], x2 = z[b0 + 2 * h], x3 = z[b0 + 3 * h];
+                const float2 w1 = tw_get(tw, pos * (P >> (st + 1)), inverse);
+                const float2 w2a = tw_get(tw, pos * (P >> (st + 2)), inverse);
+                const float2 w2b = tw_get(tw, (pos + h) * (P >> (st + 2)), inverse);
+                const float2 x0 = z[b0], x1 = z[b0 + h], x2 = z[b0 + 2 * h], x3 = z[b0 + 3 * h];
                 float2 c = cmul(x1, w1);
-                float2 y0 = make_float2(x0.x + c.x, x0.y + c.y), y1 = make_float2(x0.x - c.x, x0.y - c.y);
+                const float2 y0 = bfly_add(x0, c), y1 = bfly_sub(x0, c);
                 c = cmul(x3, w1);
-                float2 y2 = make_float2(x2.x + c.x, x2.y + c.y), y3 = make_float2(x2.x - c.x, x2.y - c.y);
+                const float2 y2 = bfly_add(x2, c), y3 = bfly_sub(x2, c);
                 c = cmul(y2, w2a);
-                z[b0] = make_float2(y0.x + c.x, y0.y + c.y);
-                z[b0 + 2 * h] = make_float2(y0.x - c.x, y0.y - c.y);
+                z[b0] = bfly_add(y0, c);
+                z[b0 + 2 * h] = bfly_sub(y0, c);
                 c = cmul(y3, w2b);
-                z[b0 + h] = make_float2(y1.x + c.x, y1.y + c.y);
-                z[b0 + 3 * h] = make_float2(y1.x - c.x, y1.y - c.y);
-            }
-            st += 2;
-        } else {
-            const int half = 1 << st;
-            const int half_total = P >> 1;
-            const int tstride = P >> (st + 1);
-            for (int t = threadIdx.x; t < nq * half_total; t += BS) {
-                const int q = t / half_total, b = t - q * half_total;
-                const int grp = b >> st, pos = b & (half - 1);
-                const int i0 = (grp << (st + 1)) + pos, i1 = i0 + half;
-                float2 w = tw[pos * tstride];
-                if (inverse) w.y = -w.y;
-                float2* z = Z + q * P;
+                z[b0 + h] = bfly_add(y1, c);
+                z[b0 + 3 * h] = bfly_sub(y1, c);
+            } else {
+                const int i0 = (g << (st + 1)) + pos, i1 = i0 + h;
+                const float2 w = tw_get(tw, pos * (P >> (st + 1)), inverse);
                 const float2 a = z[i0], c = cmul(z[i1], w);
-                z[i0] = make_float2(a.x + c.x, a.y + c.y);
-                z[i1] = make_float2(a.x - c.x, a.y - c.y);
+                z[i0] = bfly_add(a, c);
+                z[i1] = bfly_sub(a, c);
             }
-            st += 1;
         }
+        st += ns;
         __syncthreads();
     }
 }
@@ -189,28 +223,15 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
         const int q = t / H, f = t - q * H;
         const int j0 = 2 * q, j1 = 2 * q + 1;
         float2 y0 = make_float2(0.f, 0.f), y1 = make_float2(0.f, 0.f);
-        // the spectra come from L2: issue a group's loads together, then its FMAs in order (one
-        // round trip per group of 8 depth rows instead of one per row; same sums, same order)
-        for (int l0 = 0; l0 < nxi; l0 += 8) {
-            float g0v[8], g1v[8];
-#pragma unroll
-            for (int d = 0; d < 8; ++d) {
-                const int l = l0 + d;
-                g0v[d] = (l < nxi) ? __ldg(G + ((size_t)(j0 * nxi + l)) * H + f) : 0.f;
-                g1v[d] = (l < nxi && j1 < nxi) ? __ldg(G + ((size_t)(j1 * nxi + l)) * H + f) : 0.f;
-            }
-#pragma unroll
-            for (int d = 0; d < 8; ++d) {
-                const int l = l0 + d;
-                if (l < nxi) {
-                    const float2 x = S.X[l * H + f];
-                    y0.x = fmaf(g0v[d], x.x, y0.x);
-                    y0.y = fmaf(g0v[d], x.y, y0.y);
-                    if (j1 < nxi) {
-                        y1.x = fmaf(g1v[d], x.x, y1.x);
-                        y1.y = fmaf(g1v[d], x.y, y1.y);
-                    }
-                }
+        for (int l = 0; l < nxi; ++l) {
+            const float2 x = S.X[l * H + f];
+            const float g0 = __ldg(G + ((size_t)(j0 * nxi + l)) * H + f);
+            y0.x = fmaf(g0, x.x, y0.x);
+            y0.y = fmaf(g0, x.y, y0.y);
+            if (j1 < nxi) {
+                const float g1 = __ldg(G + ((size_t)(j1 * nxi + l)) * H + f);
+                y1.x = fmaf(g1, x.x, y1.x);
+                y1.y = fmaf(g1, x.y, y1.y);
             }
         }
         // W[f] = Y0[f] + i Y1[f]; W[P-f] = conj(Y0[f]) + i conj(Y1[f])
@@ -243,11 +264,16 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
             k[i] = fma(-bi * vi * psi2, dpsi, dtau) / fma(ai, psi2, m.eta);
             k[N + i] = dpsi;
         } else {
+            // ψ1 = exp((f0 + b ln(v0 θ / L)) / a) / (2 v0) = exp(c1 + (b/a) ln θ), ψ2 = σ ψ1 / hypot(1, v ψ1)
+            // as one reciprocal square root; the per-patch constants replace three serial divisions
+            // (each FP64 step of this chain costs a warp 64 cycles on this chip)
             const double tht = th[i];
-            const double psi1 = exp((m.f0 + bi * log(m.v0 * fmax(0.0, tht) / Li)) / ai) / (2.0 * m.v0);
-            const double psi2 = ps[i] * psi1 / hypot(1.0, vi * psi1);
-            const double dth = 1.0 - vi * tht / Li;
-            k[i] = (dtau - bi / tht * vi * psi2 * dth) / (ai * psi2 + m.eta);
+            (void)Li;
+            const double psi1 = exp(fma(m.boa[i], log(fmax(0.0, tht)), pc[i]));
+            const double vp = vi * psi1;
+            const double psi2 = ps[i] * psi1 * rsqrt(fma(vp, vp, 1.0));
+            const double dth = fma(-vi * tht, m.iL[i], 1.0);
+            k[i] = fma(-bi * vi * psi2, dth / tht, dtau) / fma(ai, psi2, m.eta);
             k[N + i] = dth;
         }
         k[2 * N + i] = vi;
@@ -269,21 +295,43 @@ struct EnsCtl {
     double psi_prev[5], psi[6], beta[6], g[7];
 };
 
+// this step's ψ, β and Adams weights (the oracle's orc_abm_coefficients, same operations): in
+// registers with compile-time bounds, the independent divisions h / ψ_{j-1} issued together and
+// 1/q as constants, written to the shared control block once
 __device__ __forceinline__ void ens_abm_coef(EnsCtl& c, double h) {
     const int k = c.k;
     c.kq = k;
-    c.psi[0] = h;
-    for (int i = 1; i < k; ++i) c.psi[i] = h + c.psi_prev[i - 1];
-    c.beta[0] = 1.0;
-    for (int i = 1; i < k; ++i) c.beta[i] = c.beta[i - 1] * c.psi[i - 1] / c.psi_prev[i - 1];
-    double cq[8] = {0};
-    for (int q = 1; q <= k + 1; ++q) cq[q] = 1.0 / q;
-    c.g[0] = cq[1];
-    for (int j = 1; j <= k; ++j) {
-        const double r = h / c.psi[j - 1];
-        for (int q = 1; q <= k + 1 - j; ++q) cq[q] = cq[q] - cq[q + 1] * r;
-        c.g[j] = cq[1];
+    double psi[5], beta[5], r[5];
+    psi[0] = h;
+#pragma unroll
+    for (int i = 1; i < 5; ++i) psi[i] = (i < k) ? h + c.psi_prev[i - 1] : 1.0;
+#pragma unroll
+    for (int j = 0; j < 5; ++j) r[j] = h / psi[j];
+    beta[0] = 1.0;
+#pragma unroll
+    for (int i = 1; i < 5; ++i) beta[i] = (i < k) ? beta[i - 1] * psi[i - 1] / c.psi_prev[i - 1] : 0.0;
+    double cq[8] = {0.0, 1.0, 1.0 / 2, 1.0 / 3, 1.0 / 4, 1.0 / 5, 1.0 / 6, 0.0};
+#pragma unroll
+    for (int q = 1; q <= 6; ++q)
+        if (q > k + 1) cq[q] = 0.0;
+    double g[6];
+    g[0] = cq[1];
+#pragma unroll
+    for (int j = 1; j <= 5; ++j) {
+        if (j <= k) {
+#pragma unroll
+            for (int q = 1; q <= 5; ++q)
+                if (q <= k + 1 - j) cq[q] = cq[q] - cq[q + 1] * r[j - 1];
+        }
+        g[j] = cq[1];
     }
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        c.psi[i] = psi[i];
+        c.beta[i] = beta[i];
+    }
+#pragma unroll
+    for (int j = 0; j < 6; ++j) c.g[j] = g[j];
 }
 
 // ALG 0: Tsit5 (6 RHS per step); ALG 1: VCABM5 (PECE: 1 RHS per step + 1 per accepted step;
@@ -464,10 +512,15 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
                 float* xb = S.xr + (size_t)(rx & 1) * N;
                 for (int i = lo + threadIdx.x; i < hi; i += BS) {
                     double acc[3] = {0.0, 0.0, 0.0};
-                    for (int j = 0; j < kq; ++j) {
-                        const double bj = c.beta[j], gj = c.g[j];
+                    // compile-time bounds: the stage pointers stay in registers and every load of
+                    // the differences issues before the first FMA needs one (same sums, same order)
 #pragma unroll
-                        for (int comp = 0; comp < 3; ++comp) acc[comp] = fma(gj, bj * kk[j][comp * N + i], acc[comp]);
+                    for (int j = 0; j < 5; ++j) {
+                        if (j < kq) {
+                            const double bj = c.beta[j], gj = c.g[j];
+#pragma unroll
+                            for (int comp = 0; comp < 3; ++comp) acc[comp] = fma(gj, bj * kk[j][comp * N + i], acc[comp]);
+                        }
                     }
                     const double vnew = u[i] + dt * acc[0];
                     y[i] = vnew;
@@ -497,7 +550,9 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
                     for (int comp = 0; comp < 3; ++comp) {
                         const int g = comp * N + i;
                         double sacc = 0.0;
-                        for (int j = 0; j < kq; ++j) sacc += c.beta[j] * kk[j][g];
+#pragma unroll
+                        for (int j = 0; j < 5; ++j)
+                            if (j < kq) sacc += c.beta[j] * kk[j][g];
                         const double pk = kk[6][g] - sacc;
                         const double yn = y[g] + dt * gk * pk;
                         un[g] = yn;
@@ -642,17 +697,27 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
             ens_rhs<BS>(m, A, S, un, kk[6], lo, hi, clus ? xb : nullptr);
             ++rx;
             const int kq = c.kq;
+            // the old differences are loaded before any is overwritten (the stage buffers are
+            // distinct arrays): one round trip instead of one per order, same arithmetic
             for (int comp = 0; comp < 3; ++comp)
                 for (int i = lo + threadIdx.x; i < hi; i += BS) {
                     const int g = comp * N + i;
+                    double old[5];
+#pragma unroll
+                    for (int j = 0; j < 5; ++j) old[j] = (j < kq) ? kk[j][g] : 0.0;
                     double nw = kk[6][g];
-                    for (int j = 0; j < kq; ++j) {
-                        const double old = kk[j][g];
-                        kk[j][g] = nw;
-                        nw = nw - c.beta[j] * old;
+                    const double un_g = un[g];
+#pragma unroll
+                    for (int j = 0; j < 5; ++j) {
+                        if (j < kq) {
+                            kk[j][g] = nw;
+                            nw = nw - c.beta[j] * old[j];
+                        }
                     }
-                    kk[kq][g] = nw;
-                    u[g] = un[g];
+#pragma unroll
+                    for (int j = 1; j <= 5; ++j)
+                        if (j == kq) kk[j][g] = nw;
+                    u[g] = un_g;
                 }
         }
     }
