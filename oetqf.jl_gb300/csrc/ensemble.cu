@@ -54,6 +54,7 @@ struct EnsSmem {
     double* pr;     // 2 x (nch + 1): error-norm sums of every 32-patch chunk + rank 0's stop flag
     uint64_t* mb;   // mbarriers: received slip rates (buffers 0, 1), received norms (2, 3)
     float* xr;      // 2 x N: v - vpl of every patch (clusters: own slice + the peers' pushes)
+    const float* G; // the model's real spectra: a shared-memory copy (EnsArgs::gsm) or global memory
 };
 
 // ---- cluster exchange: st.async pushes into the peers' shared memory, completing a transaction
@@ -193,7 +194,7 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
     const double* th = y + N;
     // pack rows (2q, 2q+1) as real/imag, zero padded, in bit-reversed order
     for (int t = threadIdx.x; t < nq * P; t += BS) {
-        const int q = t / P, i = t - q * P;
+        const int q = t >> logP, i = t & (P - 1);
         float re = 0.f, im = 0.f;
         if (i < nx) {
             if (xin) {
@@ -218,7 +219,7 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
     __syncthreads();
     // Y_j[f] = sum_l G[j,l,f] X_l[f] (G real); repack (2q, 2q+1) as Y_2q + i Y_2q+1 with Hermitian fill,
     // bit-reversed for the inverse transform
-    const float* G = m.ghat;
+    const float* G = S.G;
     for (int t = threadIdx.x; t < nq * H; t += BS) {
         const int q = t / H, f = t - q * H;
         const int j0 = 2 * q, j1 = 2 * q + 1;
@@ -355,6 +356,7 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
     // each rank owns whole 32-patch chunks, so the error norm below sums the same chunks in the
     // same order whatever the cluster and block sizes: a model's trajectory does not depend on them
     const int nch = (N + 31) / 32;
+    const double inv3n = 1.0 / (double)(3 * N);  // the RMS error norm's 1/n, once per launch
     const int lo = 32 * (int)((long long)nch * rank / csize);
     const int hi = min(N, 32 * (int)((long long)nch * (rank + 1) / csize));
     const int nq = (m.nxi + 1) / 2, H = m.P / 2 + 1;
@@ -367,6 +369,14 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
     S.pr = reinterpret_cast<double*>(S.tw + m.P / 2);
     S.mb = reinterpret_cast<uint64_t*>(S.pr + 2 * (nch + 1));
     S.xr = reinterpret_cast<float*>(S.mb + 4);
+    S.G = m.ghat;
+    if (A.gsm) {  // the spectra read every RHS: one copy per launch into shared memory
+        const size_t off = (reinterpret_cast<uintptr_t>(S.xr + 2 * (size_t)N) + 15) & ~(uintptr_t)15;
+        float* gs = reinterpret_cast<float*>(off);
+        const int ng = m.nxi * m.nxi * (m.P / 2 + 1);
+        for (int t = threadIdx.x; t < ng; t += BS) gs[t] = m.ghat[t];
+        S.G = gs;  // visible to every thread after the barrier below
+    }
     for (int t = threadIdx.x; t < m.P / 2; t += BS) {
         double sn, cs;
         sincospi(2.0 * t / m.P, &sn, &cs);
@@ -595,7 +605,7 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
         }
         if (threadIdx.x == 0 && ALG == 1) {
             const double tot = red[0];
-            double EEst = sqrt(tot / (double)(3 * N));
+            double EEst = sqrt(tot * inv3n);
             if (!isfinite(EEst)) EEst = INFINITY;
             const int kq = c.kq;
             // step factor 0.8 EEst^(-1/(k+1)) within [0.2, 2] (at most 0.8 after a rejection), in FP32
@@ -636,7 +646,7 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
         }
         if (threadIdx.x == 0 && ALG == 0) {
             const double tot = red[0];
-            double EEst = sqrt(tot / (double)(3 * N));
+            double EEst = sqrt(tot * inv3n);
             if (!isfinite(EEst)) EEst = INFINITY;
             const double beta1 = 0.14, beta2 = 0.08, gam = 0.9, qmin = 0.2, qmax = 10.0;
             // the PI gain factors EEst^β1 and qold^β2 only shape the next dt: FP32 (a serial FP64
@@ -807,9 +817,19 @@ static int launch_cluster(const EnsArgs& A, int nmod, int csize, size_t smem, cu
 }
 
 int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtmax, double dtmin,
-                   unsigned long long budget_ns, int block, size_t smem, cudaStream_t main, int alg) {
+                   unsigned long long budget_ns, int block, size_t smem, cudaStream_t main, int alg,
+                   size_t gbytes) {
     EnsArgs A{};
     A.alg = alg;
+    // once the active models' CTAs fit one per SM (the regrouped tail), give each CTA room for its
+    // model's spectra (the mixing then reads shared memory instead of L2; same values, same sums)
+    long long ctas = 0;
+    for (int g = 0; g < 4; ++g) ctas += (long long)L.count[g] << g;
+    A.gsm = 0;
+    if (gbytes > 0 && ctas <= sm_count() && smem + gbytes + 16 <= 200 * 1024) {
+        A.gsm = 1;
+        smem += gbytes + 16;
+    }
     A.models = L.models; A.nmodels = L.n; A.order = L.order;
     A.reltol = reltol; A.abstol = abstol; A.dtmax = dtmax; A.dtmin = dtmin;
     A.budget = 1 << 20;
@@ -898,6 +918,7 @@ struct gbc_ensemble {
     std::vector<int> has_gf, has_props;
     long long total_n = 0, total_st = 0;
     size_t smem = 0;
+    size_t gbytes = 0;  // spectra of the largest model, bytes
     cudaStream_t stream = nullptr;
     EnsModel* d_models = nullptr;
     float* ghat = nullptr;
@@ -984,6 +1005,7 @@ int gbc_ensemble_create(int nmodels, const int* nx, const int* nxi, gbc_ensemble
         os += (long long)nxi[i] * nxi[i] * (m.P / 2 + 1);
         const size_t sm = ens_smem_bytes(nx[i], nxi[i], m.P);
         e->smem = std::max(e->smem, sm);
+        e->gbytes = std::max(e->gbytes, sizeof(float) * ens_ghat_floats(m));
     }
     e->total_n = on;
     e->total_st = os;
@@ -1199,7 +1221,7 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
         int rc = 0;
         for (int k = 0; k < 2 && !rc; ++k)
             rc = ens_run_groups(e->lp, o->reltol, o->abstol, o->dtmax, o->dtmin, 100000000ull, e->block, e->smem, s,
-                                o->alg);
+                                o->alg, e->gbytes);
         cudaError_t ce = cudaStreamEndCapture(s, &g);
         if (rc) return rc;
         GBC_CUDA(ce);

@@ -37,6 +37,7 @@ struct EnsArgs {
     double reltol, abstol, dtmax, dtmin;
     int budget;                      // step cap per launch and model
     unsigned long long budget_ns;    // wall-clock budget per launch (all models stay busy until done)
+    int gsm;                         // 1: each CTA copies its model's spectra into shared memory
 };
 
 
@@ -65,8 +66,11 @@ void ens_launch_destroy(EnsLaunch& L);
 int ens_launch_prepare(EnsLaunch& L, EnsModel* d_models, const EnsModel* host, int n, int maxc, int boost,
                        cudaStream_t s);
 // one persistent launch per group: each model runs until done or budget_ns of wall clock
+// gbytes > 0: the largest model's spectra in bytes; when every CTA of the grouping gets an SM to
+// itself and the spectra fit beside the FFT buffers, the launches stage them in shared memory
 int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtmax, double dtmin,
-                   unsigned long long budget_ns, int block, size_t smem, cudaStream_t main, int alg = 0);
+                   unsigned long long budget_ns, int block, size_t smem, cudaStream_t main, int alg = 0,
+                   size_t gbytes = 0);
 // θ <-> ln θ on the state of every descriptor with `logged` set
 int ens_theta(EnsModel* d_models, int n, int to_log, cudaStream_t s);
 void count_launches(long long n);
