@@ -88,6 +88,19 @@ __device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, unsigned parity
     return false;
 }
 
+// 1/x by Newton-Raphson (r <- r + r (1 - x r), the relative error squaring each step) from the
+// correctly rounded FP32 reciprocal of x rounded to FP32 (error < 2^-23): two steps leave ~2^-90
+// plus FP64 rounding, about 1 ulp -- four dependent FMAs where an FP64 division is a long chain of
+// dependent FP64 instructions at 64 cycles each on this chip. Outside FP32's normal range the
+// seed is not usable and the plain division runs.
+__device__ __forceinline__ double ens_rcp(double x) {
+    const double ax = fabs(x);
+    if (!(ax > 1e-36 && ax < 1e36)) return 1.0 / x;
+    double r = (double)__frcp_rn(__double2float_rn(x));
+    r = fma(r, fma(-x, r, 1.0), r);
+    return fma(r, fma(-x, r, 1.0), r);
+}
+
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 
 // in-place radix-2 DIT FFT of nq arrays of length P already in bit-reversed order; forward uses
@@ -226,11 +239,13 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
         float2 y0 = make_float2(0.f, 0.f), y1 = make_float2(0.f, 0.f);
         for (int l = 0; l < nxi; ++l) {
             const float2 x = S.X[l * H + f];
-            const float g0 = __ldg(G + ((size_t)(j0 * nxi + l)) * H + f);
+            // generic loads: G is global memory or a shared-memory copy (a read-only-path load
+            // would accept only global addresses)
+            const float g0 = G[((size_t)(j0 * nxi + l)) * H + f];
             y0.x = fmaf(g0, x.x, y0.x);
             y0.y = fmaf(g0, x.y, y0.y);
             if (j1 < nxi) {
-                const float g1 = __ldg(G + ((size_t)(j1 * nxi + l)) * H + f);
+                const float g1 = G[((size_t)(j1 * nxi + l)) * H + f];
                 y1.x = fmaf(g1, x.x, y1.x);
                 y1.y = fmaf(g1, x.y, y1.y);
             }
@@ -274,7 +289,7 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
             const double vp = vi * psi1;
             const double psi2 = ps[i] * psi1 * rsqrt(fma(vp, vp, 1.0));
             const double dth = fma(-vi * tht, m.iL[i], 1.0);
-            k[i] = fma(-bi * vi * psi2, dth / tht, dtau) / fma(ai, psi2, m.eta);
+            k[i] = fma(-bi * vi * psi2, dth * ens_rcp(tht), dtau) * ens_rcp(fma(ai, psi2, m.eta));
             k[N + i] = dth;
         }
         k[2 * N + i] = vi;
@@ -307,10 +322,10 @@ __device__ __forceinline__ void ens_abm_coef(EnsCtl& c, double h) {
 #pragma unroll
     for (int i = 1; i < 5; ++i) psi[i] = (i < k) ? h + c.psi_prev[i - 1] : 1.0;
 #pragma unroll
-    for (int j = 0; j < 5; ++j) r[j] = h / psi[j];
+    for (int j = 0; j < 5; ++j) r[j] = h * ens_rcp(psi[j]);
     beta[0] = 1.0;
 #pragma unroll
-    for (int i = 1; i < 5; ++i) beta[i] = (i < k) ? beta[i - 1] * psi[i - 1] / c.psi_prev[i - 1] : 0.0;
+    for (int i = 1; i < 5; ++i) beta[i] = (i < k) ? beta[i - 1] * (psi[i - 1] * ens_rcp(c.psi_prev[i - 1])) : 0.0;
     double cq[8] = {0.0, 1.0, 1.0 / 2, 1.0 / 3, 1.0 / 4, 1.0 / 5, 1.0 / 6, 0.0};
 #pragma unroll
     for (int q = 1; q <= 6; ++q)
@@ -568,7 +583,7 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
                         un[g] = yn;
                         const double sc = (comp == 1 && m.log_theta) ? A.abstol + A.reltol
                                                                      : A.abstol + A.reltol * fmax(fabs(u[g]), fabs(yn));
-                        r[comp] = (ce * pk) / sc;
+                        r[comp] = (ce * pk) * ens_rcp(sc);
                         bad |= !isfinite(yn);
                     }
                     ss = fma(r[0], r[0], ss);
@@ -605,12 +620,14 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
         }
         if (threadIdx.x == 0 && ALG == 1) {
             const double tot = red[0];
-            double EEst = sqrt(tot * inv3n);
+            // the squared RMS norm decides acceptance (sqrt is monotonic and sqrt(1) = 1, so
+            // EEst <= 1 exactly when EEst^2 <= 1); the step factor needs only FP32
+            double EEst = tot * inv3n;
             if (!isfinite(EEst)) EEst = INFINITY;
             const int kq = c.kq;
             // step factor 0.8 EEst^(-1/(k+1)) within [0.2, 2] (at most 0.8 after a rejection), in FP32
             // like the PI gains; acceptance compares the FP64 norm
-            const double fac = 0.8 * (double)exp2f(-log2f((float)EEst) / (float)(kq + 1));
+            const double fac = 0.8 * (double)exp2f(-0.5f * log2f((float)EEst) / (float)(kq + 1));
             c.iters += 1;
             double dtn;
             int acc = 0;
