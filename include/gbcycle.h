@@ -239,14 +239,17 @@ int gbc_ensemble_set_fault_props(gbc_ensemble* e, int model, const double* a, co
 int gbc_ensemble_set_block(gbc_ensemble* e, int threads);
 /* Integrate ψ = ln θ internally (default on; the caller's state keeps θ). */
 int gbc_ensemble_set_log_theta(gbc_ensemble* e, int on);
-/* Largest thread-block cluster per model (1, 2, 4 or 8; default 8). Models above 600 patches
+/* Largest thread-block cluster per model (1, 2, 4, 8 or 16; default 16). Models above 600 patches
  * are split over a cluster of CTAs (2 up to 1200 patches, 4 up to 2400, 8 beyond): each CTA owns
  * a slice of the patches for the friction update, the stages and the error norm, and the CTAs
- * meet at cluster barriers. A model's trajectory does not depend on its cluster or block size
- * (its error norm is summed over fixed 32-patch chunks in a fixed order). */
+ * exchange slip rates and error-norm sums through distributed shared memory. Regrouping may give
+ * the last few running models 16-CTA clusters, where that non-portable size can be resident. A
+ * model's trajectory does not depend on its cluster or block size (its error norm is summed over
+ * fixed 32-patch chunks in a fixed order). */
 int gbc_ensemble_set_max_cluster(gbc_ensemble* e, int ctas);
 /* Regrouping (default on): as models finish, the ones still running move to larger clusters
- * (every model at least 2, 4 or 8 CTAs once the active models times that size fit the SMs). */
+ * (every model at least 2, 4, 8 or 16 CTAs once twice the active models times that size fit the
+ * SMs). */
 int gbc_ensemble_set_regroup(gbc_ensemble* e, int on);
 /* The flat state is the concatenation over models of (v, θ, δ); model i starts at
  * gbc_ensemble_state_offset(e, i). Each model integrates from t0[i] to t1[i]; stats has one entry

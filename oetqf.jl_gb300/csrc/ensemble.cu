@@ -17,6 +17,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <set>
+#include <utility>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -311,43 +314,52 @@ struct EnsCtl {
     double psi_prev[5], psi[6], beta[6], g[7];
 };
 
-// this step's ψ, β and Adams weights (the oracle's orc_abm_coefficients, same operations): in
-// registers with compile-time bounds, the independent divisions h / ψ_{j-1} issued together and
-// 1/q as constants, written to the shared control block once
-__device__ __forceinline__ void ens_abm_coef(EnsCtl& c, double h) {
+__device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+// This step's ψ, β and Adams weights (the oracle's orc_abm_coefficients: ψ_0 = h, ψ_i = h + ψ'_{i-1},
+// β_i = β_{i-1} ψ_{i-1} / ψ'_{i-1}, g_j from c_0(q) = 1/q, c_j(q) = c_{j-1}(q) - c_{j-1}(q+1) h/ψ_{j-1}),
+// computed by the lanes of one warp: FP64 instructions issue about once per 64 cycles per warp on
+// this chip whatever the number of active lanes, so lane j takes ψ_j, h/ψ_j and ψ_j/ψ'_j with one
+// instruction sequence for all, lane q holds c(q) of the recursion (each order one FMA for all q),
+// and β is a running product over lanes. Same recursion, same order of products as the serial form.
+__device__ __forceinline__ void ens_abm_coef(EnsCtl& c, double h, int lane) {
     const int k = c.k;
-    c.kq = k;
-    double psi[5], beta[5], r[5];
-    psi[0] = h;
+    const double psi = (lane == 0) ? h : (lane < k) ? h + c.psi_prev[lane - 1] : 1.0;
+    // one reciprocal for all lanes: lanes 0..4 invert ψ_lane, lanes 8..12 invert ψ'_{lane-8}
+    const double den = (lane < 5) ? psi : (lane >= 8 && lane < 8 + k - 1) ? c.psi_prev[lane - 8] : 1.0;
+    const double rc = ens_rcp(den);
+    const double rj = h * rc;                          // lane j < 5: h / ψ_j
+    const double ratio = psi * shfl_d(rc, (lane + 8) & 31);  // lane i: ψ_i / ψ'_i
+    double beta = 1.0;                                 // lane i: β_i = Π_{m < i} ψ_m / ψ'_m
 #pragma unroll
-    for (int i = 1; i < 5; ++i) psi[i] = (i < k) ? h + c.psi_prev[i - 1] : 1.0;
-#pragma unroll
-    for (int j = 0; j < 5; ++j) r[j] = h * ens_rcp(psi[j]);
-    beta[0] = 1.0;
-#pragma unroll
-    for (int i = 1; i < 5; ++i) beta[i] = (i < k) ? beta[i - 1] * (psi[i - 1] * ens_rcp(c.psi_prev[i - 1])) : 0.0;
-    double cq[8] = {0.0, 1.0, 1.0 / 2, 1.0 / 3, 1.0 / 4, 1.0 / 5, 1.0 / 6, 0.0};
+    for (int m = 0; m < 4; ++m) {
+        const double rm = shfl_d(ratio, m);
+        if (lane > m && lane < k) beta *= rm;
+    }
+    const double inv_q[8] = {0.0, 1.0, 1.0 / 2, 1.0 / 3, 1.0 / 4, 1.0 / 5, 1.0 / 6, 0.0};
+    double cq = 0.0;                                   // lane q (1..k+1): c(q)
 #pragma unroll
     for (int q = 1; q <= 6; ++q)
-        if (q > k + 1) cq[q] = 0.0;
-    double g[6];
-    g[0] = cq[1];
+        if (lane == q && q <= k + 1) cq = inv_q[q];
+    double g = 0.0;                                    // lane j ends with g_j
+    {
+        const double g0 = shfl_d(cq, 1);               // every lane shuffles; lane 0 keeps g_0
+        if (lane == 0) g = g0;
+    }
 #pragma unroll
     for (int j = 1; j <= 5; ++j) {
-        if (j <= k) {
-#pragma unroll
-            for (int q = 1; q <= 5; ++q)
-                if (q <= k + 1 - j) cq[q] = cq[q] - cq[q + 1] * r[j - 1];
-        }
-        g[j] = cq[1];
+        const double r = shfl_d(rj, j - 1);            // h / ψ_{j-1}
+        const double up = shfl_d(cq, (lane + 1) & 31); // c(q+1) before this order's update
+        if (j <= k && lane >= 1 && lane <= k + 1 - j) cq = cq - up * r;
+        const double gj = shfl_d(cq, 1);
+        if (lane == j) g = gj;
     }
-#pragma unroll
-    for (int i = 0; i < 5; ++i) {
-        c.psi[i] = psi[i];
-        c.beta[i] = beta[i];
+    if (lane < 5) {
+        c.psi[lane] = psi;
+        c.beta[lane] = beta;
     }
-#pragma unroll
-    for (int j = 0; j < 6; ++j) c.g[j] = g[j];
+    if (lane < 6) c.g[lane] = g;
+    if (lane == 0) c.kq = k;
 }
 
 // ALG 0: Tsit5 (6 RHS per step); ALG 1: VCABM5 (PECE: 1 RHS per step + 1 per accepted step;
@@ -530,7 +542,7 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
             // with the error chunks; f at the corrected point and the Phi update after acceptance
             // every thread is done with the last step's beta (its Phi update) before thread 0 rewrites it
             __syncthreads();
-            if (threadIdx.x == 0) ens_abm_coef(c, dt);
+            if (warp == 0) ens_abm_coef(c, dt, lane);
             __syncthreads();
             const int kq = c.kq;
             {
@@ -795,17 +807,17 @@ int ens_csize(int N, int maxc, int boost) {
     return c < maxc ? c : maxc;
 }
 
-int ens_boost(int nactive) {
+int ens_boost(int nactive, int maxb) {
     int b = 1;
-    while (b < 8 && (long long)nactive * b * 2 <= sm_count()) b *= 2;
+    while (b < maxb && (long long)nactive * b * 2 <= sm_count()) b *= 2;
     return b;
 }
 
 // the models still running, grouped by cluster size
-void ens_groups(const EnsModel* models, int n, int maxc, int boost, std::vector<int>& order, int first[4],
-                int count[4]) {
+void ens_groups(const EnsModel* models, int n, int maxc, int boost, std::vector<int>& order, int first[kEnsGroups],
+                int count[kEnsGroups]) {
     order.clear();
-    for (int g = 0; g < 4; ++g) {
+    for (int g = 0; g < kEnsGroups; ++g) {
         first[g] = (int)order.size();
         for (int i = 0; i < n; ++i)
             if (!models[i].done && ens_csize(models[i].N, maxc, boost) == (1 << g)) order.push_back(i);
@@ -813,10 +825,49 @@ void ens_groups(const EnsModel* models, int n, int maxc, int boost, std::vector<
     }
 }
 
+static int allow_cluster16(const void* kern) {
+    int dev = 0;
+    GBC_CUDA(cudaGetDevice(&dev));
+    static std::mutex mu;
+    static std::set<std::pair<const void*, int>> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count(std::make_pair(kern, dev))) return 0;
+    GBC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    done.insert(std::make_pair(kern, dev));
+    return 0;
+}
+
+bool ens_cluster16_ok(size_t smem, int alg) {
+    void (*kern)(EnsArgs) = (alg == 1) ? k_ensemble<512, 1> : k_ensemble<512, 0>;
+    if (allow_cluster16((const void*)kern) || set_smem_limit((const void*)kern, (int)smem)) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(16);
+    cfg.blockDim = dim3(512);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 16;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, (const void*)kern, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return n >= 1;
+}
+
 template <int BS>
 static int launch_cluster(const EnsArgs& A, int nmod, int csize, size_t smem, cudaStream_t s) {
     void (*kern)(EnsArgs) = (A.alg == 1) ? k_ensemble<BS, 1> : k_ensemble<BS, 0>;
     if (int rc = set_smem_limit((const void*)kern, (int)smem)) return rc;
+    if (csize > 8)
+        if (int rc = allow_cluster16((const void*)kern)) return rc;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(nmod * csize));
     cfg.blockDim = dim3(BS);
@@ -841,7 +892,7 @@ int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtma
     // once the active models' CTAs fit one per SM (the regrouped tail), give each CTA room for its
     // model's spectra (the mixing then reads shared memory instead of L2; same values, same sums)
     long long ctas = 0;
-    for (int g = 0; g < 4; ++g) ctas += (long long)L.count[g] << g;
+    for (int g = 0; g < kEnsGroups; ++g) ctas += (long long)L.count[g] << g;
     A.gsm = 0;
     if (gbytes > 0 && ctas <= sm_count() && smem + gbytes + 16 <= 200 * 1024) {
         A.gsm = 1;
@@ -853,7 +904,7 @@ int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtma
     A.budget_ns = budget_ns;
     GBC_CUDA(cudaEventRecord(L.fork, main));
     int launched = 0;
-    for (int g = 0; g < 4; ++g) {
+    for (int g = 0; g < kEnsGroups; ++g) {
         if (L.count[g] == 0) continue;
         cudaStream_t s = L.aux[g];
         GBC_CUDA(cudaStreamWaitEvent(s, L.fork, 0));
@@ -879,7 +930,7 @@ int ens_launch_create(EnsLaunch& L, int capacity) {
     L.cap = capacity;
     GBC_CUDA(cudaMalloc(&L.order, sizeof(int) * capacity));
     GBC_CUDA(cudaEventCreateWithFlags(&L.fork, cudaEventDisableTiming));
-    for (int g = 0; g < 4; ++g) {
+    for (int g = 0; g < kEnsGroups; ++g) {
         GBC_CUDA(cudaStreamCreateWithFlags(&L.aux[g], cudaStreamNonBlocking));
         GBC_CUDA(cudaEventCreateWithFlags(&L.join[g], cudaEventDisableTiming));
     }
@@ -889,7 +940,7 @@ int ens_launch_create(EnsLaunch& L, int capacity) {
 void ens_launch_destroy(EnsLaunch& L) {
     if (L.order) cudaFree((void*)L.order);
     if (L.fork) cudaEventDestroy(L.fork);
-    for (int g = 0; g < 4; ++g) {
+    for (int g = 0; g < kEnsGroups; ++g) {
         if (L.aux[g]) cudaStreamDestroy(L.aux[g]);
         if (L.join[g]) cudaEventDestroy(L.join[g]);
     }
@@ -943,7 +994,8 @@ struct gbc_ensemble {
            *u = nullptr, *y = nullptr, *un = nullptr;
     double* k[7] = {};
     int block = 256;
-    int max_cluster = 8;
+    int max_cluster = 16;
+    int c16 = -1;  // whether 16-CTA clusters can launch (-1: not yet checked)
     int regroup = 1;
     int log_theta = 1;
     cudaGraphExec_t exec = nullptr;
@@ -1173,7 +1225,8 @@ int gbc_ensemble_set_block(gbc_ensemble* e, int threads) {
 }
 
 int gbc_ensemble_set_max_cluster(gbc_ensemble* e, int ctas) {
-    if (!e || (ctas != 1 && ctas != 2 && ctas != 4 && ctas != 8)) return fail(GBC_EINVAL, "cluster size must be 1, 2, 4 or 8");
+    if (!e || (ctas != 1 && ctas != 2 && ctas != 4 && ctas != 8 && ctas != 16))
+        return fail(GBC_EINVAL, "cluster size must be 1, 2, 4, 8 or 16");
     e->max_cluster = ctas;
     return 0;
 }
@@ -1252,7 +1305,11 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
         for (int i = 0; i < e->n; ++i) a += (e->host[i].done == 0);
         return a;
     };
-    int boost = e->regroup ? ens_boost(active()) : 1;
+    // the largest cluster the regrouped tail may use: 16 CTAs where that non-portable size can be
+    // resident with the tail's shared memory (FFT buffers + spectra), else 8
+    if (e->c16 < 0) e->c16 = ens_cluster16_ok(e->smem + e->gbytes + 16, o->alg) ? 1 : 0;
+    const int maxb = std::min(e->max_cluster, e->c16 ? 16 : 8);
+    int boost = e->regroup ? ens_boost(active(), maxb) : 1;
     if (int rc = capture(boost)) return rc;
     for (;;) {
         GBC_CUDA(cudaGraphLaunch(e->exec, s));
@@ -1260,7 +1317,7 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
         GBC_CUDA(cudaStreamSynchronize(s));
         const int na = active();
         if (na == 0) break;
-        const int nb = e->regroup ? ens_boost(na) : 1;
+        const int nb = e->regroup ? ens_boost(na, maxb) : 1;
         if (nb != boost) {
             boost = nb;
             if (int rc = capture(boost)) return rc;

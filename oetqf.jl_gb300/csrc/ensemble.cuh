@@ -46,20 +46,25 @@ int ens_prepare_model(EnsModel& m, int nx, int nxi, size_t* smem_bytes);
 size_t ens_ghat_floats(const EnsModel& m);
 // real spectra of the model's circulant kernels from its real Toeplitz kernel (device)
 int ens_ghat(const double* st_dev, const EnsModel& m, float* ghat_dev, cudaStream_t s);
+// cluster sizes 1, 2, 4, 8 and 16 CTAs (16 is a non-portable size, used only where it can launch)
+constexpr int kEnsGroups = 5;
 // Models are grouped by cluster size (1, 2, 4 or 8 CTAs per model, from the patch count); each
 // group is one persistent cluster launch on its own stream, forked from and joined to `main`.
 struct EnsLaunch {
     EnsModel* models = nullptr;
     int n = 0, cap = 0;
     const int* order = nullptr;  // device: model indices grouped by cluster size
-    int first[4] = {0, 0, 0, 0}, count[4] = {0, 0, 0, 0};
-    cudaStream_t aux[4] = {nullptr, nullptr, nullptr, nullptr};
-    cudaEvent_t fork = nullptr, join[4] = {nullptr, nullptr, nullptr, nullptr};
+    int first[kEnsGroups] = {0, 0, 0, 0, 0}, count[kEnsGroups] = {0, 0, 0, 0, 0};
+    cudaStream_t aux[kEnsGroups] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join[kEnsGroups] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 // cluster size of a model of N patches: by size, at least `boost`, at most maxc
 int ens_csize(int N, int maxc, int boost);
-// the cluster size every model may use when nactive models share the SMs (1, 2, 4 or 8)
-int ens_boost(int nactive);
+// the cluster size every model may use when nactive models share the SMs (1, 2, ... up to maxb)
+int ens_boost(int nactive, int maxb = 8);
+// whether 16-CTA clusters of the 512-thread ensemble kernel with smem bytes of shared memory each
+// can be resident (non-portable cluster size; sets the kernel attribute that allows it)
+bool ens_cluster16_ok(size_t smem, int alg);
 int ens_launch_create(EnsLaunch& L, int capacity);
 void ens_launch_destroy(EnsLaunch& L);
 // groups the models of `host` that are not done (uploads their order)
