@@ -612,9 +612,15 @@ def run_sweep(args):
 
 
 def run_ensemble_profile(args):
-    """Short ensemble run for ncu captures of the persistent kernel (0.01 yr of the 256 models)."""
+    """Short ensemble runs for ncu captures of the persistent kernel: 0.01 yr of the 256 models, or
+    with --profile-member i that model of the headline ensemble alone (regrouped onto the largest
+    cluster it may use, as the slowest models run once the others have finished) for
+    --profile-steps integrator steps."""
     from oetqf_gb300.ensemble import Ensemble
-    models = fault_ensemble(n_models=256, years=0.01)
+    years = 0.01 if args.profile_member < 0 else ENSEMBLE_WINDOW_YR
+    models = fault_ensemble(n_models=256, years=years)
+    if args.profile_member >= 0:
+        models = [models[args.profile_member]]
     e = Ensemble([(mm.mf.nx, mm.mf.nξ) for mm in models])
     for i, mm in enumerate(models):
         e.assemble(i, mm.mf, mm.lam, mm.mu)
@@ -622,9 +628,14 @@ def run_ensemble_profile(args):
     u0 = np.zeros(e.state_len)
     for i, mm in enumerate(models):
         u0[e.offsets[i]:e.offsets[i] + mm.u0.size] = mm.u0
-    e.set_block(256)
-    u, st = e.integrate(u0, 0.0, 0.01 * YEAR, **SOLVER)
-    print(json.dumps({"profile_ensemble": True, "steps": int(sum(s.naccept + s.nreject for s in st))}))
+    if args.profile_member >= 0:
+        e.set_log_theta(args.alg != "VCABM5")
+        e.set_block(512)
+        u, st = e.integrate(u0, 0.0, 1e15, maxiters=args.profile_steps, alg=args.alg, **SOLVER)
+    else:
+        e.set_block(256)
+        u, st = e.integrate(u0, 0.0, 0.01 * YEAR, alg=args.alg, **SOLVER)
+    print(json.dumps({"profile_ensemble": True, "models": len(models), "steps": int(sum(s.naccept + s.nreject for s in st))}))
 
 
 def run_serving(args):
@@ -1116,6 +1127,9 @@ def main():
     ap.add_argument("--years", type=float, default=0.0,
                     help="override the window (default line: %g yr) or a workload's horizon" % ENSEMBLE_WINDOW_YR)
     ap.add_argument("--profile-precision", default="f64", choices=["f64", "bf16", "f16", "df64"])
+    ap.add_argument("--profile-member", type=int, default=-1,
+                    help="ensemble-profile: that model of the headline ensemble alone")
+    ap.add_argument("--profile-steps", type=int, default=2000, help="ensemble-profile: integrator steps")
     ap.add_argument("--variants", type=int, default=32, help="property variants of the sweep workload")
     ap.add_argument("--engine", default="umma", choices=["simt", "umma"], help="product engine of the sweep workload")
     ap.add_argument("--fault-product", action="store_true", help="sweep workload: fault-fault rows on the tensor cores too")
