@@ -314,52 +314,43 @@ struct EnsCtl {
     double psi_prev[5], psi[6], beta[6], g[7];
 };
 
-__device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
-
-// This step's ψ, β and Adams weights (the oracle's orc_abm_coefficients: ψ_0 = h, ψ_i = h + ψ'_{i-1},
-// β_i = β_{i-1} ψ_{i-1} / ψ'_{i-1}, g_j from c_0(q) = 1/q, c_j(q) = c_{j-1}(q) - c_{j-1}(q+1) h/ψ_{j-1}),
-// computed by the lanes of one warp: FP64 instructions issue about once per 64 cycles per warp on
-// this chip whatever the number of active lanes, so lane j takes ψ_j, h/ψ_j and ψ_j/ψ'_j with one
-// instruction sequence for all, lane q holds c(q) of the recursion (each order one FMA for all q),
-// and β is a running product over lanes. Same recursion, same order of products as the serial form.
-__device__ __forceinline__ void ens_abm_coef(EnsCtl& c, double h, int lane) {
+// this step's ψ, β and Adams weights (the oracle's orc_abm_coefficients, same operations): in
+// registers with compile-time bounds, the independent divisions h / ψ_{j-1} issued together and
+// 1/q as constants, written to the shared control block once
+__device__ __forceinline__ void ens_abm_coef(EnsCtl& c, double h) {
     const int k = c.k;
-    const double psi = (lane == 0) ? h : (lane < k) ? h + c.psi_prev[lane - 1] : 1.0;
-    // one reciprocal for all lanes: lanes 0..4 invert ψ_lane, lanes 8..12 invert ψ'_{lane-8}
-    const double den = (lane < 5) ? psi : (lane >= 8 && lane < 8 + k - 1) ? c.psi_prev[lane - 8] : 1.0;
-    const double rc = ens_rcp(den);
-    const double rj = h * rc;                          // lane j < 5: h / ψ_j
-    const double ratio = psi * shfl_d(rc, (lane + 8) & 31);  // lane i: ψ_i / ψ'_i
-    double beta = 1.0;                                 // lane i: β_i = Π_{m < i} ψ_m / ψ'_m
+    c.kq = k;
+    double psi[5], beta[5], r[5];
+    psi[0] = h;
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
-        const double rm = shfl_d(ratio, m);
-        if (lane > m && lane < k) beta *= rm;
-    }
-    const double inv_q[8] = {0.0, 1.0, 1.0 / 2, 1.0 / 3, 1.0 / 4, 1.0 / 5, 1.0 / 6, 0.0};
-    double cq = 0.0;                                   // lane q (1..k+1): c(q)
+    for (int i = 1; i < 5; ++i) psi[i] = (i < k) ? h + c.psi_prev[i - 1] : 1.0;
+#pragma unroll
+    for (int j = 0; j < 5; ++j) r[j] = h * ens_rcp(psi[j]);
+    beta[0] = 1.0;
+#pragma unroll
+    for (int i = 1; i < 5; ++i) beta[i] = (i < k) ? beta[i - 1] * (psi[i - 1] * ens_rcp(c.psi_prev[i - 1])) : 0.0;
+    double cq[8] = {0.0, 1.0, 1.0 / 2, 1.0 / 3, 1.0 / 4, 1.0 / 5, 1.0 / 6, 0.0};
 #pragma unroll
     for (int q = 1; q <= 6; ++q)
-        if (lane == q && q <= k + 1) cq = inv_q[q];
-    double g = 0.0;                                    // lane j ends with g_j
-    {
-        const double g0 = shfl_d(cq, 1);               // every lane shuffles; lane 0 keeps g_0
-        if (lane == 0) g = g0;
-    }
+        if (q > k + 1) cq[q] = 0.0;
+    double g[6];
+    g[0] = cq[1];
 #pragma unroll
     for (int j = 1; j <= 5; ++j) {
-        const double r = shfl_d(rj, j - 1);            // h / ψ_{j-1}
-        const double up = shfl_d(cq, (lane + 1) & 31); // c(q+1) before this order's update
-        if (j <= k && lane >= 1 && lane <= k + 1 - j) cq = cq - up * r;
-        const double gj = shfl_d(cq, 1);
-        if (lane == j) g = gj;
+        if (j <= k) {
+#pragma unroll
+            for (int q = 1; q <= 5; ++q)
+                if (q <= k + 1 - j) cq[q] = cq[q] - cq[q + 1] * r[j - 1];
+        }
+        g[j] = cq[1];
     }
-    if (lane < 5) {
-        c.psi[lane] = psi;
-        c.beta[lane] = beta;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        c.psi[i] = psi[i];
+        c.beta[i] = beta[i];
     }
-    if (lane < 6) c.g[lane] = g;
-    if (lane == 0) c.kq = k;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) c.g[j] = g[j];
 }
 
 // ALG 0: Tsit5 (6 RHS per step); ALG 1: VCABM5 (PECE: 1 RHS per step + 1 per accepted step;
@@ -542,7 +533,7 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
             // with the error chunks; f at the corrected point and the Phi update after acceptance
             // every thread is done with the last step's beta (its Phi update) before thread 0 rewrites it
             __syncthreads();
-            if (warp == 0) ens_abm_coef(c, dt, lane);
+            if (threadIdx.x == 0) ens_abm_coef(c, dt);
             __syncthreads();
             const int kq = c.kq;
             {
