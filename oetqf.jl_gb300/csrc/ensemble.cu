@@ -234,10 +234,14 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
     }
     __syncthreads();
     // Y_j[f] = sum_l G[j,l,f] X_l[f] (G real); repack (2q, 2q+1) as Y_2q + i Y_2q+1 with Hermitian fill,
-    // bit-reversed for the inverse transform
+    // bit-reversed for the inverse transform. Only the row pairs holding this CTA's patches [lo, hi)
+    // are mixed and transformed back (a cluster rank's slice spans one or two depth rows): the
+    // forward spectra of every row are needed, the traction rates of the other rows are not.
     const float* G = S.G;
-    for (int t = threadIdx.x; t < nq * H; t += BS) {
-        const int q = t / H, f = t - q * H;
+    const int qlo = (hi > lo) ? (lo / nx) >> 1 : 0;
+    const int nqr = (hi > lo) ? (((hi - 1) / nx) >> 1) - qlo + 1 : 0;
+    for (int t = threadIdx.x; t < nqr * H; t += BS) {
+        const int q = qlo + t / H, f = t - (q - qlo) * H;
         const int j0 = 2 * q, j1 = 2 * q + 1;
         float2 y0 = make_float2(0.f, 0.f), y1 = make_float2(0.f, 0.f);
         for (int l = 0; l < nxi; ++l) {
@@ -259,7 +263,7 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
         if (f > 0 && f < P - f) W[__brev(P - f) >> (32 - logP)] = make_float2(y0.x + y1.y, -y0.y + y1.x);
     }
     __syncthreads();
-    fft_many<BS>(S.Z, nq, P, logP, S.tw, 1);
+    fft_many<BS>(S.Z + (size_t)qlo * P, nqr, P, logP, S.tw, 1);
     const double invP = 1.0 / P;
     const double* pa = m.a;
     const double* pb = m.b;
