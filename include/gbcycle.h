@@ -352,8 +352,9 @@ typedef struct gbc_server_info {
     long long cache_hits, cache_misses;
 } gbc_server_info;
 
-/* A server admitting requests while their estimated device footprint fits hbm_budget_bytes
- * (arrival order). A native scheduler thread owns all GPU work. */
+/* A server admitting requests while their estimated device footprint fits hbm_budget_bytes, in
+ * arrival order, except that fault-only requests (megabytes) that fit run ahead of a queued
+ * request that does not fit yet. A native scheduler thread owns all GPU work. */
 int gbc_server_create(double hbm_budget_bytes, const gbc_solver_opts* batch_opts, gbc_server** out);
 int gbc_server_submit(gbc_server* s, const gbc_request* req, long long* id);
 /* Blocks until request id finishes; writes its final state into u_out (host, may be NULL). */

@@ -369,9 +369,7 @@ static void scheduler(gbc_server* s) {
     while (true) {
         // admit from the head of the queue while the HBM budget allows (arrival order); cached
         // Green's functions are reused, idle ones evicted when the head would not fit otherwise
-        while (!s->queue.empty() && acquire(s, *s->queue.front())) {
-            std::shared_ptr<Req> r = s->queue.front();
-            s->queue.pop_front();
+        auto start = [&](std::shared_ptr<Req> r) {
             s->peak = std::max(s->peak, s->in_use);
             r->t_admit = s->now();
             if (r->ne > 0) {
@@ -389,6 +387,23 @@ static void scheduler(gbc_server* s) {
                 } else {
                     s->batch_active.push_back(r);
                 }
+            }
+        };
+        while (!s->queue.empty() && acquire(s, *s->queue.front())) {
+            std::shared_ptr<Req> r = s->queue.front();
+            s->queue.pop_front();
+            start(r);
+        }
+        // a head that does not fit yet (a mantle request waiting for gigabytes) keeps its place;
+        // fault-only requests queued behind it that fit now (megabytes each) run around it, so a
+        // stream of small requests is not held behind one large one
+        for (size_t i = 1; i < s->queue.size() && i <= 256;) {
+            std::shared_ptr<Req> r = s->queue[i];
+            if (r->ne == 0 && acquire(s, *r)) {
+                s->queue.erase(s->queue.begin() + (long)i);
+                start(r);
+            } else {
+                ++i;
             }
         }
         // reap finished mantle workers
