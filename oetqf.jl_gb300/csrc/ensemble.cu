@@ -112,55 +112,6 @@ __device__ __forceinline__ double ens_rcp_in_range(double x) {
     return fma(r, fma(-x, r, 1.0), r);
 }
 
-// FP64 exp and log with short dependency chains for the friction update (each dependent FP64
-// instruction costs a warp about 64 cycles on this chip). exp: x = k ln2 + r with k = rint(x log2 e)
-// and r reduced by two FMAs against ln2 split into a double and its remainder (Cody and Waite's
-// reduction with a fused multiply-add), |r| <= ln2/2; e^r by its Taylor series to degree 13
-// (remainder < 5e-18) evaluated by Estrin's scheme; times 2^k built from the exponent bits.
-// log: x = 2^e m with m in [sqrt(1/2), sqrt(2)), ln m = 2 atanh(s), s = (m - 1)/(m + 1), |s| < 0.172,
-// by the series 2 s sum s^(2n)/(2n+1) to n = 10 (Estrin in s^2); plus e ln2. Both are within a few
-// units in the last place (tests/test_fp64_exp_log.py replays them against 40-digit references);
-// arguments outside the normal range take the library functions.
-constexpr double kLn2Hi = 0.6931471805599453, kLn2Lo = 2.3190468138462996e-17, kLog2e = 1.4426950408889634;
-
-__device__ __forceinline__ double ens_exp(double x) {
-    if (!(x > -745.2 && x < 709.78)) return exp(x);
-    const double k = rint(x * kLog2e);
-    double r = fma(-k, kLn2Hi, x);
-    r = fma(-k, kLn2Lo, r);
-    const double r2 = r * r, r4 = r2 * r2, r8 = r4 * r4;
-    const double p0 = fma(1.0, r, 1.0), p1 = fma(1.0 / 6, r, 1.0 / 2), p2 = fma(1.0 / 120, r, 1.0 / 24),
-                 p3 = fma(1.0 / 5040, r, 1.0 / 720), p4 = fma(1.0 / 362880, r, 1.0 / 40320),
-                 p5 = fma(1.0 / 39916800, r, 1.0 / 3628800), p6 = fma(1.0 / 6227020800.0, r, 1.0 / 479001600);
-    const double q0 = fma(p1, r2, p0), q1 = fma(p3, r2, p2), q2 = fma(p5, r2, p4);
-    const double s0 = fma(q1, r4, q0), s1 = fma(p6, r4, q2);
-    const double e = fma(s1, r8, s0);
-    const int ki = (int)k;
-    if (ki >= -1020 && ki <= 1020) return e * __longlong_as_double((long long)(ki + 1023) << 52);
-    const int h = ki / 2;
-    return e * __longlong_as_double((long long)(h + 1023) << 52) * __longlong_as_double((long long)(ki - h + 1023) << 52);
-}
-
-__device__ __forceinline__ double ens_log(double x) {
-    if (!(x >= 2.2250738585072014e-308 && x <= 1.7976931348623157e308)) return log(x);
-    const long long bits = __double_as_longlong(x);
-    int e = (int)((bits >> 52) & 0x7ff) - 1023;
-    double m = __longlong_as_double((bits & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
-    if (m > 1.4142135623730951) {
-        m *= 0.5;
-        e += 1;
-    }
-    const double s = (m - 1.0) * ens_rcp_in_range(m + 1.0);
-    const double z = s * s, z2 = z * z, z4 = z2 * z2, z8 = z4 * z4;
-    const double p0 = fma(1.0 / 3, z, 1.0), p1 = fma(1.0 / 7, z, 1.0 / 5), p2 = fma(1.0 / 11, z, 1.0 / 9),
-                 p3 = fma(1.0 / 15, z, 1.0 / 13), p4 = fma(1.0 / 19, z, 1.0 / 17);
-    const double q0 = fma(p1, z2, p0), q1 = fma(p3, z2, p2), q2 = fma(1.0 / 21, z2, p4);
-    const double t0 = fma(q1, z4, q0);
-    const double P = fma(q2, z8, t0);
-    const double de = (double)e;
-    return fma(de, kLn2Hi, fma(de, kLn2Lo, (s + s) * P));
-}
-
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 
 // in-place radix-2 DIT FFT of nq arrays of length P already in bit-reversed order; forward uses
@@ -349,7 +300,7 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
             // (each FP64 step of this chain costs a warp 64 cycles on this chip)
             const double tht = th[i];
             (void)Li;
-            const double psi1 = ens_exp(fma(m.boa[i], ens_log(fmax(0.0, tht)), pc[i]));
+            const double psi1 = exp(fma(m.boa[i], log(fmax(0.0, tht)), pc[i]));
             const double vp = vi * psi1;
             const double psi2 = ps[i] * psi1 * rsqrt(fma(vp, vp, 1.0));
             const double dth = fma(-vi * tht, m.iL[i], 1.0);
