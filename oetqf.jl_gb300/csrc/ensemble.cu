@@ -818,12 +818,14 @@ int ens_boost(int nactive, int maxb) {
 
 // the models still running, grouped by cluster size
 void ens_groups(const EnsModel* models, int n, int maxc, int boost, std::vector<int>& order, int first[kEnsGroups],
-                int count[kEnsGroups]) {
+                int count[kEnsGroups], const int* want) {
     order.clear();
     for (int g = 0; g < kEnsGroups; ++g) {
         first[g] = (int)order.size();
-        for (int i = 0; i < n; ++i)
-            if (!models[i].done && ens_csize(models[i].N, maxc, boost) == (1 << g)) order.push_back(i);
+        for (int i = 0; i < n; ++i) {
+            const int cs = want ? want[i] : ens_csize(models[i].N, maxc, boost);
+            if (!models[i].done && cs == (1 << g)) order.push_back(i);
+        }
         count[g] = (int)order.size() - first[g];
     }
 }
@@ -876,13 +878,20 @@ static int launch_cluster(const EnsArgs& A, int nmod, int csize, size_t smem, cu
     cfg.blockDim = dim3(BS);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
-    cudaLaunchAttribute at[1];
+    cudaLaunchAttribute at[2];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = (unsigned)csize;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
+    // larger clusters hold the stiffest models: their CTAs are dispatched first
+    int least = 0, greatest = 0;
+    GBC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    int lg = 0;
+    while ((1 << lg) < csize) ++lg;
+    at[1].id = cudaLaunchAttributePriority;
+    at[1].val.priority = std::max(greatest, least - lg);
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = 2;
     GBC_CUDA(cudaLaunchKernelEx(&cfg, kern, A));
     return 0;
 }
@@ -907,7 +916,7 @@ int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtma
     A.budget_ns = budget_ns;
     GBC_CUDA(cudaEventRecord(L.fork, main));
     int launched = 0;
-    for (int g = 0; g < kEnsGroups; ++g) {
+    for (int g = kEnsGroups - 1; g >= 0; --g) {  // the largest clusters first
         if (L.count[g] == 0) continue;
         cudaStream_t s = L.aux[g];
         GBC_CUDA(cudaStreamWaitEvent(s, L.fork, 0));
@@ -952,10 +961,10 @@ void ens_launch_destroy(EnsLaunch& L) {
 
 // uploads the grouped order of the models (host descriptors) and fills the group table
 int ens_launch_prepare(EnsLaunch& L, EnsModel* d_models, const EnsModel* host, int n, int maxc, int boost,
-                       cudaStream_t s) {
+                       cudaStream_t s, const int* want) {
     if (n > L.cap) return fail(GBC_EINVAL, "ensemble launch capacity exceeded");
     std::vector<int> order;
-    ens_groups(host, n, maxc, boost, order, L.first, L.count);
+    ens_groups(host, n, maxc, boost, order, L.first, L.count, want);
     L.models = d_models;
     L.n = n;
     if (!order.empty())
@@ -1286,14 +1295,20 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
     // still running move to larger clusters (their FP64 friction, stage and error-norm work spreads
     // over more SMs; the trajectory does not depend on the cluster size) and the graph is captured
     // again for the new grouping.
+    std::vector<int> want;  // per-model cluster sizes (regrouping), empty: the size rule
     auto capture = [&](int boost) -> int {
         if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
-        if (int rc = ens_launch_prepare(e->lp, e->d_models, e->host.data(), e->n, e->max_cluster, boost, s)) return rc;
+        if (int rc = ens_launch_prepare(e->lp, e->d_models, e->host.data(), e->n, e->max_cluster, boost, s,
+                                        want.empty() ? nullptr : want.data()))
+            return rc;
+        // one-CTA models that outnumber the SMs run at 256 threads, two per SM (128 registers a
+        // thread), so that all of them stay resident; a model's steps do not depend on it
+        const int block0 = (e->lp.count[0] > sm_count()) ? 256 : e->block;
         cudaGraph_t g;
         GBC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         int rc = 0;
         for (int k = 0; k < 2 && !rc; ++k)
-            rc = ens_run_groups(e->lp, o->reltol, o->abstol, o->dtmax, o->dtmin, 100000000ull, e->block, e->smem, s,
+            rc = ens_run_groups(e->lp, o->reltol, o->abstol, o->dtmax, o->dtmin, 100000000ull, block0, e->smem, s,
                                 o->alg, e->gbytes);
         cudaError_t ce = cudaStreamEndCapture(s, &g);
         if (rc) return rc;
@@ -1312,7 +1327,39 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
     // resident with the tail's shared memory (FFT buffers + spectra), else 8
     if (e->c16 < 0) e->c16 = ens_cluster16_ok(e->smem + e->gbytes + 16, o->alg) ? 1 : 0;
     const int maxb = std::min(e->max_cluster, e->c16 ? 16 : 8);
+    // Regrouping. The 512-thread cluster kernel holds one CTA per SM (128 registers a thread), so a
+    // grouping that asks for more CTAs than SMs time-slices every model, the stiffest included. With
+    // regrouping on, every model starts on one CTA (all resident); after each launch the models
+    // whose step count in it is within 4x of the busiest one's take the largest cluster that still
+    // fits one CTA per SM (their per-step latency sets the makespan), the others one CTA, or the
+    // common boost once few models remain. A model's trajectory does not depend on its cluster.
+    auto sizes = [&](int nb, const std::vector<long long>& d) {
+        std::vector<int> w(e->n, nb);
+        long long used = 0, dmax = 0;
+        std::vector<std::pair<long long, int>> hot;
+        for (int i = 0; i < e->n; ++i)
+            if (!e->host[i].done) {
+                used += nb;
+                dmax = std::max(dmax, d[i]);
+                hot.emplace_back(d[i], i);
+            }
+        std::sort(hot.begin(), hot.end(), [](const std::pair<long long, int>& x, const std::pair<long long, int>& y) {
+            return x.first > y.first || (x.first == y.first && x.second < y.second);
+        });
+        for (const auto& h : hot) {
+            if (dmax <= 0 || h.first * 4 < dmax) break;
+            for (int c = maxb; c > nb; c >>= 1)
+                if (used + (c - nb) <= sm_count()) {
+                    w[h.second] = c;
+                    used += c - nb;
+                    break;
+                }
+        }
+        return w;
+    };
+    std::vector<long long> prev(e->n, 0), dsteps(e->n, 0);
     int boost = e->regroup ? ens_boost(active(), maxb) : 1;
+    if (e->regroup) want = sizes(boost, dsteps);
     if (int rc = capture(boost)) return rc;
     for (;;) {
         GBC_CUDA(cudaGraphLaunch(e->exec, s));
@@ -1320,9 +1367,19 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
         GBC_CUDA(cudaStreamSynchronize(s));
         const int na = active();
         if (na == 0) break;
-        const int nb = e->regroup ? ens_boost(na, maxb) : 1;
-        if (nb != boost) {
+        if (!e->regroup) continue;
+        for (int i = 0; i < e->n; ++i) {
+            const long long st = e->host[i].naccept + e->host[i].nreject;
+            dsteps[i] = st - prev[i];
+            prev[i] = st;
+        }
+        const int nb = ens_boost(na, maxb);
+        std::vector<int> w = sizes(nb, dsteps);
+        bool changed = (nb != boost);
+        for (int i = 0; i < e->n && !changed; ++i) changed = !e->host[i].done && w[i] != want[i];
+        if (changed) {
             boost = nb;
+            want = w;
             if (int rc = capture(boost)) return rc;
         }
     }

@@ -67,9 +67,10 @@ int ens_boost(int nactive, int maxb = 8);
 bool ens_cluster16_ok(size_t smem, int alg);
 int ens_launch_create(EnsLaunch& L, int capacity);
 void ens_launch_destroy(EnsLaunch& L);
-// groups the models of `host` that are not done (uploads their order)
+// groups the models of `host` that are not done (uploads their order); want (host, may be null)
+// gives each model's cluster size instead of the size rule
 int ens_launch_prepare(EnsLaunch& L, EnsModel* d_models, const EnsModel* host, int n, int maxc, int boost,
-                       cudaStream_t s);
+                       cudaStream_t s, const int* want = nullptr);
 // one persistent launch per group: each model runs until done or budget_ns of wall clock
 // gbytes > 0: the largest model's spectra in bytes; when every CTA of the grouping gets an SM to
 // itself and the spectra fit beside the FFT buffers, the launches stage them in shared memory
