@@ -239,18 +239,27 @@ int gbc_ensemble_set_fault_props(gbc_ensemble* e, int model, const double* a, co
 int gbc_ensemble_set_block(gbc_ensemble* e, int threads);
 /* Integrate ψ = ln θ internally (default on; the caller's state keeps θ). */
 int gbc_ensemble_set_log_theta(gbc_ensemble* e, int on);
-/* Largest thread-block cluster per model (1, 2, 4, 8 or 16; default 16). Models above 600 patches
- * are split over a cluster of CTAs (2 up to 1200 patches, 4 up to 2400, 8 beyond): each CTA owns
- * a slice of the patches for the friction update, the stages and the error norm, and the CTAs
- * exchange slip rates and error-norm sums through distributed shared memory. Regrouping may give
- * the last few running models 16-CTA clusters, where that non-portable size can be resident. A
- * model's trajectory does not depend on its cluster or block size (its error norm is summed over
- * fixed 32-patch chunks in a fixed order). */
+/* Largest thread-block cluster per model (1, 2, 4, 8 or 16; default 16). A model on a cluster of
+ * CTAs is split over them: each CTA owns a slice of the patches for the friction update, the
+ * stages and the error norm, and the CTAs exchange slip rates and error-norm sums through
+ * distributed shared memory. 16-CTA clusters are used where that non-portable size can be
+ * resident. A model's trajectory does not depend on its cluster or block size (its error norm is
+ * summed over fixed 32-patch chunks in a fixed order). */
 int gbc_ensemble_set_max_cluster(gbc_ensemble* e, int ctas);
-/* Regrouping (default on): as models finish, the ones still running move to larger clusters
- * (every model at least 2, 4, 8 or 16 CTAs once twice the active models times that size fit the
- * SMs). */
+/* Regrouping (default on). Before the first launch and after every launch (about 0.2 s), the
+ * models still running are planned onto cluster sizes (gbc_ensemble_plan_clusters, with the
+ * occupancy the GPU reports for each size), so that all their CTAs are resident together; the
+ * larger clusters launch first, at a higher stream priority. Off: the size rule by patch count
+ * (one CTA up to 600 patches, 2 up to 1200, 4 up to 2400, 8 beyond). */
 int gbc_ensemble_set_regroup(gbc_ensemble* e, int on);
+/* The regrouping plan (host only, no GPU): sizes[i] = the cluster size (1, 2, 4, 8 or 16) for n
+ * models of npatch[i] patches, done[i] != 0 for finished ones (size 1), steps_left[i] = the steps
+ * left at the current step size (ties only). capacity[g] = how many clusters of 2^g CTAs the GPU
+ * holds at once (g = 0..4; 0: that size is not available). Every model starts on one CTA; then,
+ * repeatedly, the model with the largest predicted step latency moves to the next size when that
+ * saves at least 3 % and the sum over running models of 1 / capacity[log2 size] stays at most 1. */
+int gbc_ensemble_plan_clusters(int n, const int* npatch, const int* done, const double* steps_left,
+                               const int* capacity, int* sizes);
 /* The flat state is the concatenation over models of (v, θ, δ); model i starts at
  * gbc_ensemble_state_offset(e, i). Each model integrates from t0[i] to t1[i]; stats has one entry
  * per model. The _dev variant takes a device pointer. */

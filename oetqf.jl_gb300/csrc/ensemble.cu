@@ -810,6 +810,47 @@ int ens_csize(int N, int maxc, int boost) {
     return c < maxc ? c : maxc;
 }
 
+// Predicted microseconds per VCABM5 step of an N-patch model on a cluster of c CTAs of 512 threads:
+// a fixed part (step control and barriers), the model's patches spread over the cluster (FFT
+// convolution, friction, error norm) and the cluster's exchanges. A fit to single-model timings on
+// a GB300 (N = 400 to 1960, c = 1 to 16, within 10 %); it only ranks the models when they are
+// planned onto clusters.
+double ens_step_us(int N, int c) {
+    int lg = 0;
+    while ((1 << lg) < c) ++lg;
+    return 16.0 + (double)N / (11.7 * c) + 2.0 * lg;
+}
+
+// Cluster sizes for the n models (done[i] != 0: finished, size 1): every model starts on one
+// CTA; then, repeatedly, the model with the largest predicted step latency (ties: more steps left,
+// then the lower index) moves to the next size, if that saves at least 3 % and the grouping stays
+// within the GPU: the sum over models of 1 / cap[log2 size] at most one, cap[g] the clusters of
+// 1 << g CTAs it holds at once (0: size not available).
+void ens_plan(int n, const int* N, const int* done, const double* left, const double cap[kEnsGroups], int* w) {
+    double used = 0.0;
+    for (int i = 0; i < n; ++i) {
+        w[i] = 1;
+        if (!done[i]) used += cap[0] > 0 ? 1.0 / cap[0] : 1.0;
+    }
+    for (;;) {
+        int best = -1, bg = 0;
+        double bl = -1.0, bkey = 0.0;
+        for (int i = 0; i < n; ++i) {
+            if (done[i]) continue;
+            int g = 0;
+            while ((1 << g) < w[i]) ++g;
+            if (g + 1 >= kEnsGroups || cap[g + 1] <= 0 || cap[g] <= 0) continue;
+            const double l = ens_step_us(N[i], w[i]);
+            if (ens_step_us(N[i], 2 * w[i]) > 0.97 * l) continue;
+            if (used + 1.0 / cap[g + 1] - 1.0 / cap[g] > 1.0 + 1e-9) continue;
+            if (l > bl || (l == bl && left[i] > bkey)) { best = i; bg = g; bl = l; bkey = left[i]; }
+        }
+        if (best < 0) break;
+        used += 1.0 / cap[bg + 1] - 1.0 / cap[bg];
+        w[best] *= 2;
+    }
+}
+
 int ens_boost(int nactive, int maxb) {
     int b = 1;
     while (b < maxb && (long long)nactive * b * 2 <= sm_count()) b *= 2;
@@ -842,19 +883,23 @@ static int allow_cluster16(const void* kern) {
     return 0;
 }
 
-bool ens_cluster16_ok(size_t smem, int alg) {
-    void (*kern)(EnsArgs) = (alg == 1) ? k_ensemble<512, 1> : k_ensemble<512, 0>;
-    if (allow_cluster16((const void*)kern) || set_smem_limit((const void*)kern, (int)smem)) {
+// how many clusters of csize CTAs (block threads each, smem bytes of dynamic shared memory) the
+// GPU holds at once; clusters live inside one GPC, so this is less than SMs / csize for large sizes
+int ens_max_clusters(int csize, int block, size_t smem, int alg) {
+    void (*kern)(EnsArgs) = (block == 128) ? ((alg == 1) ? k_ensemble<128, 1> : k_ensemble<128, 0>)
+                          : (block == 256) ? ((alg == 1) ? k_ensemble<256, 1> : k_ensemble<256, 0>)
+                                           : ((alg == 1) ? k_ensemble<512, 1> : k_ensemble<512, 0>);
+    if ((csize > 8 && allow_cluster16((const void*)kern)) || set_smem_limit((const void*)kern, (int)smem)) {
         cudaGetLastError();
-        return false;
+        return 0;
     }
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(16);
-    cfg.blockDim = dim3(512);
+    cfg.gridDim = dim3((unsigned)csize);
+    cfg.blockDim = dim3((unsigned)block);
     cfg.dynamicSmemBytes = smem;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = 16;
+    at[0].val.clusterDim.x = (unsigned)csize;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
@@ -862,10 +907,12 @@ bool ens_cluster16_ok(size_t smem, int alg) {
     int n = 0;
     if (cudaOccupancyMaxActiveClusters(&n, (const void*)kern, &cfg) != cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return 0;
     }
-    return n >= 1;
+    return n;
 }
+
+bool ens_cluster16_ok(size_t smem, int alg) { return ens_max_clusters(16, 512, smem, alg) >= 1; }
 
 template <int BS>
 static int launch_cluster(const EnsArgs& A, int nmod, int csize, size_t smem, cudaStream_t s) {
@@ -901,15 +948,12 @@ int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtma
                    size_t gbytes) {
     EnsArgs A{};
     A.alg = alg;
-    // once the active models' CTAs fit one per SM (the regrouped tail), give each CTA room for its
-    // model's spectra (the mixing then reads shared memory instead of L2; same values, same sums)
+    // Room for each CTA's copy of its model's spectra (the mixing then reads shared memory instead
+    // of L2; same values, same sums): always in the 512-thread cluster groups, which hold a whole
+    // SM's registers anyway; in the one-CTA group once every active CTA has an SM to itself.
     long long ctas = 0;
     for (int g = 0; g < kEnsGroups; ++g) ctas += (long long)L.count[g] << g;
-    A.gsm = 0;
-    if (gbytes > 0 && ctas <= sm_count() && smem + gbytes + 16 <= 200 * 1024) {
-        A.gsm = 1;
-        smem += gbytes + 16;
-    }
+    const bool gfit = gbytes > 0 && smem + gbytes + 16 <= 200 * 1024;
     A.models = L.models; A.nmodels = L.n; A.order = L.order;
     A.reltol = reltol; A.abstol = abstol; A.dtmax = dtmax; A.dtmin = dtmin;
     A.budget = 1 << 20;
@@ -924,10 +968,12 @@ int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtma
         // models split over clusters are the large ones: 512 threads per CTA measured best for them;
         // the one-CTA group uses the (autotuned) block size
         const int b = (g > 0) ? 512 : block;
+        A.gsm = gfit && (g > 0 || ctas <= sm_count()) ? 1 : 0;
+        const size_t sg = A.gsm ? smem + gbytes + 16 : smem;
         int rc;
-        if (b == 128) rc = launch_cluster<128>(A, L.count[g], 1 << g, smem, s);
-        else if (b == 512) rc = launch_cluster<512>(A, L.count[g], 1 << g, smem, s);
-        else rc = launch_cluster<256>(A, L.count[g], 1 << g, smem, s);
+        if (b == 128) rc = launch_cluster<128>(A, L.count[g], 1 << g, sg, s);
+        else if (b == 512) rc = launch_cluster<512>(A, L.count[g], 1 << g, sg, s);
+        else rc = launch_cluster<256>(A, L.count[g], 1 << g, sg, s);
         if (rc) return rc;
         GBC_CUDA(cudaEventRecord(L.join[g], s));
         GBC_CUDA(cudaStreamWaitEvent(main, L.join[g], 0));
@@ -1249,6 +1295,19 @@ int gbc_ensemble_set_regroup(gbc_ensemble* e, int on) {
     return 0;
 }
 
+int gbc_ensemble_plan_clusters(int n, const int* npatch, const int* done, const double* steps_left,
+                               const int* capacity, int* sizes) {
+    if (n < 0 || (n > 0 && (!npatch || !done || !steps_left || !capacity || !sizes)))
+        return fail(GBC_EINVAL, "null argument");
+    double cap[kEnsGroups];
+    for (int g = 0; g < kEnsGroups; ++g) {
+        if (capacity[g] < 0) return fail(GBC_EINVAL, "negative cluster capacity");
+        cap[g] = capacity[g];
+    }
+    ens_plan(n, npatch, done, steps_left, cap, sizes);
+    return 0;
+}
+
 int gbc_ensemble_set_log_theta(gbc_ensemble* e, int on) {
     if (!e) return fail(GBC_EINVAL, "null ensemble");
     e->log_theta = on ? 1 : 0;
@@ -1290,25 +1349,30 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
         if (int rc = ens_theta(e->d_models, e->n, 1, s)) return rc;
         count_launches(1);
     }
-    // A captured pair of persistent launches (one per cluster size, on forked streams, 100 ms of
-    // wall clock each), relaunched until every model reports done. As models finish, the ones
-    // still running move to larger clusters (their FP64 friction, stage and error-norm work spreads
-    // over more SMs; the trajectory does not depend on the cluster size) and the graph is captured
-    // again for the new grouping.
+    // Persistent launches (one per cluster size, on forked streams, 100 ms of wall clock each),
+    // relaunched until every model reports done. With regrouping, the models still running are
+    // planned onto cluster sizes again after every launch (their FP64 friction, stage and
+    // error-norm work spreads over more SMs; the trajectory does not depend on the cluster size).
     std::vector<int> want;  // per-model cluster sizes (regrouping), empty: the size rule
+    // one-CTA models that outnumber the SMs the clusters leave free run at 256 threads, two per
+    // SM (128 registers a thread), so that all of them stay resident; a model's steps do not
+    // depend on it
+    auto block0 = [&]() {
+        long long hot_sms = 0;
+        for (int g = 1; g < kEnsGroups; ++g) hot_sms += (long long)e->lp.count[g] << g;
+        return (e->lp.count[0] > sm_count() - hot_sms) ? 256 : e->block;
+    };
+    // the fixed size rule: a captured pair of launches, relaunched
     auto capture = [&](int boost) -> int {
         if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
-        if (int rc = ens_launch_prepare(e->lp, e->d_models, e->host.data(), e->n, e->max_cluster, boost, s,
-                                        want.empty() ? nullptr : want.data()))
+        if (int rc = ens_launch_prepare(e->lp, e->d_models, e->host.data(), e->n, e->max_cluster, boost, s, nullptr))
             return rc;
-        // one-CTA models that outnumber the SMs run at 256 threads, two per SM (128 registers a
-        // thread), so that all of them stay resident; a model's steps do not depend on it
-        const int block0 = (e->lp.count[0] > sm_count()) ? 256 : e->block;
+        const int b0 = block0();
         cudaGraph_t g;
         GBC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         int rc = 0;
         for (int k = 0; k < 2 && !rc; ++k)
-            rc = ens_run_groups(e->lp, o->reltol, o->abstol, o->dtmax, o->dtmin, 100000000ull, block0, e->smem, s,
+            rc = ens_run_groups(e->lp, o->reltol, o->abstol, o->dtmax, o->dtmin, 100000000ull, b0, e->smem, s,
                                 o->alg, e->gbytes);
         cudaError_t ce = cudaStreamEndCapture(s, &g);
         if (rc) return rc;
@@ -1327,60 +1391,63 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
     // resident with the tail's shared memory (FFT buffers + spectra), else 8
     if (e->c16 < 0) e->c16 = ens_cluster16_ok(e->smem + e->gbytes + 16, o->alg) ? 1 : 0;
     const int maxb = std::min(e->max_cluster, e->c16 ? 16 : 8);
-    // Regrouping. The 512-thread cluster kernel holds one CTA per SM (128 registers a thread), so a
-    // grouping that asks for more CTAs than SMs time-slices every model, the stiffest included. With
-    // regrouping on, every model starts on one CTA (all resident); after each launch the models
-    // whose step count in it is within 4x of the busiest one's take the largest cluster that still
-    // fits one CTA per SM (their per-step latency sets the makespan), the others one CTA, or the
-    // common boost once few models remain. A model's trajectory does not depend on its cluster.
-    auto sizes = [&](int nb, const std::vector<long long>& d) {
-        std::vector<int> w(e->n, nb);
-        long long used = 0, dmax = 0;
-        std::vector<std::pair<long long, int>> hot;
-        for (int i = 0; i < e->n; ++i)
-            if (!e->host[i].done) {
-                used += nb;
-                dmax = std::max(dmax, d[i]);
-                hot.emplace_back(d[i], i);
-            }
-        std::sort(hot.begin(), hot.end(), [](const std::pair<long long, int>& x, const std::pair<long long, int>& y) {
-            return x.first > y.first || (x.first == y.first && x.second < y.second);
-        });
-        for (const auto& h : hot) {
-            if (dmax <= 0 || h.first * 4 < dmax) break;
-            for (int c = maxb; c > nb; c >>= 1)
-                if (used + (c - nb) <= sm_count()) {
-                    w[h.second] = c;
-                    used += c - nb;
-                    break;
-                }
+    // Regrouping: the models still running are planned onto cluster sizes so that all their CTAs are
+    // resident at once (a CTA that waits for a free SM waits a whole launch). Clusters live inside
+    // one GPC, so the GPU holds fewer large clusters than SMs / size: a grouping is admitted while
+    // the sum over models of 1 / (clusters of its size the GPU holds, from the occupancy query) stays
+    // at most one. Every model starts on one CTA; then, repeatedly, the model with the largest
+    // predicted per-step latency moves to the next cluster size, if that saves at least 3 % and
+    // still fits. A model's trajectory does not depend on its cluster.
+    const bool gfit = e->gbytes > 0 && e->smem + e->gbytes + 16 <= 200 * 1024;
+    double cap[kEnsGroups];  // clusters of 1 << g CTAs the GPU holds, as launched
+    cap[0] = ens_max_clusters(1, 256, e->smem, o->alg);
+    for (int g = 1; g < kEnsGroups; ++g)
+        cap[g] = ((1 << g) <= maxb) ? ens_max_clusters(1 << g, 512, gfit ? e->smem + e->gbytes + 16 : e->smem, o->alg) : 0;
+    auto sizes = [&]() {
+        std::vector<int> N(e->n), done(e->n), w(e->n);
+        std::vector<double> left(e->n);
+        for (int i = 0; i < e->n; ++i) {
+            const EnsModel& m = e->host[i];
+            N[i] = m.N; done[i] = m.done;
+            left[i] = (m.t1 - m.t) / std::max(m.dt, 1e-300);
         }
+        ens_plan(e->n, N.data(), done.data(), left.data(), cap, w.data());
         return w;
     };
-    std::vector<long long> prev(e->n, 0), dsteps(e->n, 0);
-    int boost = e->regroup ? ens_boost(active(), maxb) : 1;
-    if (e->regroup) want = sizes(boost, dsteps);
-    if (int rc = capture(boost)) return rc;
-    for (;;) {
-        GBC_CUDA(cudaGraphLaunch(e->exec, s));
-        GBC_CUDA(cudaMemcpyAsync(e->host.data(), e->d_models, sizeof(EnsModel) * e->n, cudaMemcpyDeviceToHost, s));
-        GBC_CUDA(cudaStreamSynchronize(s));
-        const int na = active();
-        if (na == 0) break;
-        if (!e->regroup) continue;
-        for (int i = 0; i < e->n; ++i) {
-            const long long st = e->host[i].naccept + e->host[i].nreject;
-            dsteps[i] = st - prev[i];
-            prev[i] = st;
+    if (e->regroup) {
+        // One launch per cluster size per host round trip, issued to an idle GPU with the largest
+        // clusters first (and at a higher priority): a captured graph, or launches queued behind
+        // the previous ones, would leave the order in which the grids reach the GPU open, and a
+        // smaller-cluster grid placed first can split the GPCs so that a large cluster waits a
+        // whole launch for room (measured: 5 x 16 + 4 x 8 CTAs all start together largest-first,
+        // not smallest-first). The host synchronisation costs microseconds per 100 ms launch.
+        want = sizes();
+        if (int rc = ens_launch_prepare(e->lp, e->d_models, e->host.data(), e->n, e->max_cluster, 1, s, want.data()))
+            return rc;
+        for (;;) {
+            if (int rc = ens_run_groups(e->lp, o->reltol, o->abstol, o->dtmax, o->dtmin, 100000000ull, block0(),
+                                        e->smem, s, o->alg, e->gbytes))
+                return rc;
+            GBC_CUDA(cudaMemcpyAsync(e->host.data(), e->d_models, sizeof(EnsModel) * e->n, cudaMemcpyDeviceToHost, s));
+            GBC_CUDA(cudaStreamSynchronize(s));
+            if (active() == 0) break;
+            std::vector<int> w = sizes();
+            bool changed = false;
+            for (int i = 0; i < e->n && !changed; ++i) changed = !e->host[i].done && w[i] != want[i];
+            if (changed) {
+                want = w;
+                if (int rc = ens_launch_prepare(e->lp, e->d_models, e->host.data(), e->n, e->max_cluster, 1, s,
+                                                want.data()))
+                    return rc;
+            }
         }
-        const int nb = ens_boost(na, maxb);
-        std::vector<int> w = sizes(nb, dsteps);
-        bool changed = (nb != boost);
-        for (int i = 0; i < e->n && !changed; ++i) changed = !e->host[i].done && w[i] != want[i];
-        if (changed) {
-            boost = nb;
-            want = w;
-            if (int rc = capture(boost)) return rc;
+    } else {
+        if (int rc = capture(1)) return rc;
+        for (;;) {
+            GBC_CUDA(cudaGraphLaunch(e->exec, s));
+            GBC_CUDA(cudaMemcpyAsync(e->host.data(), e->d_models, sizeof(EnsModel) * e->n, cudaMemcpyDeviceToHost, s));
+            GBC_CUDA(cudaStreamSynchronize(s));
+            if (active() == 0) break;
         }
     }
     if (e->log_theta) {

@@ -62,6 +62,9 @@ struct EnsLaunch {
 int ens_csize(int N, int maxc, int boost);
 // the cluster size every model may use when nactive models share the SMs (1, 2, ... up to maxb)
 int ens_boost(int nactive, int maxb = 8);
+double ens_step_us(int N, int c);
+void ens_plan(int n, const int* N, const int* done, const double* left, const double cap[kEnsGroups], int* w);
+int ens_max_clusters(int csize, int block, size_t smem, int alg);
 // whether 16-CTA clusters of the 512-thread ensemble kernel with smem bytes of shared memory each
 // can be resident (non-portable cluster size; sets the kernel attribute that allows it)
 bool ens_cluster16_ok(size_t smem, int alg);

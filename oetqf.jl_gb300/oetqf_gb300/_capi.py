@@ -90,6 +90,8 @@ def lib():
             "gbc_ensemble_set_log_theta": [P, I],
             "gbc_ensemble_set_max_cluster": [P, I],
             "gbc_ensemble_set_regroup": [P, I],
+            "gbc_ensemble_plan_clusters": [I, ctypes.POINTER(I), ctypes.POINTER(I), PD, ctypes.POINTER(I),
+                                           ctypes.POINTER(I)],
             "gbc_hex_mesh_grid": [ctypes.POINTER(HexMesh), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)],
             "gbc_ensemble_integrate": [P, PD, PD, PD, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],
             "gbc_ensemble_integrate_dev": [P, P, PD, PD, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)],

@@ -74,6 +74,23 @@ class Ensemble:
         """Move the models still running to larger clusters as others finish (default on)."""
         C.check(C.lib().gbc_ensemble_set_regroup(self.h, int(bool(on))))
 
+    @staticmethod
+    def plan_clusters(npatch, done, steps_left, capacity):
+        """The cluster size the regrouping gives each model (host only, no GPU): npatch[i] patches,
+        done[i] finished, steps_left[i] steps left at the current step size; capacity[g] clusters of
+        2**g CTAs the GPU holds at once (g = 0..4)."""
+        npatch = np.ascontiguousarray(npatch, dtype=np.int32)
+        n = npatch.size
+        done = np.ascontiguousarray(np.broadcast_to(done, (n,)), dtype=np.int32)
+        left = np.ascontiguousarray(np.broadcast_to(steps_left, (n,)), dtype=np.float64)
+        cap = np.ascontiguousarray(capacity, dtype=np.int32)
+        if cap.size != 5:
+            raise ValueError("capacity holds the clusters of 1, 2, 4, 8 and 16 CTAs")
+        out = np.zeros(n, dtype=np.int32)
+        ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        C.check(C.lib().gbc_ensemble_plan_clusters(n, ip(npatch), ip(done), C.ptr(left), ip(cap), ip(out)))
+        return out
+
     def set_log_theta(self, on: bool):
         C.check(C.lib().gbc_ensemble_set_log_theta(self.h, int(bool(on))))
 
