@@ -55,6 +55,7 @@ struct EnsSmem {
     float2* X;
     float2* tw;
     double* pr;     // 2 x (nch + 1): error-norm sums of every 32-patch chunk + rank 0's stop flag
+    double* cp;     // 3 x nch: VCABM5 error-norm sums of the CTA's chunks, one per component
     uint64_t* mb;   // mbarriers: received slip rates (buffers 0, 1), received norms (2, 3)
     float* xr;      // 2 x N: v - vpl of every patch (clusters: own slice + the peers' pushes)
     const float* G; // the model's real spectra: a shared-memory copy (EnsArgs::gsm) or global memory
@@ -324,23 +325,39 @@ struct EnsCtl {
     // step, and this step's psi, beta and Adams weights (the oracle's orc_abm_coefficients)
     int k, kq, fails;
     double psi_prev[5], psi[6], beta[6], g[7];
+    double rat[9];  // h / psi_j (j = 0..4) and psi_{i-1} / psi_prev_{i-1} (i = 1..4), one warp each
 };
 
-// this step's ψ, β and Adams weights (the oracle's orc_abm_coefficients, same operations): in
-// registers with compile-time bounds, the independent divisions h / ψ_{j-1} issued together and
-// 1/q as constants, written to the shared control block once
+// this step's ψ, β and Adams weights (the oracle's orc_abm_coefficients, same operations), in two
+// parts. A warp issues about one FP64 instruction per 64 cycles however few lanes are active, so
+// the nine independent ratios (h / ψ_j and ψ_{i-1} / ψ_prev_{i-1}, a Newton reciprocal and a
+// product each) go to nine warps (lane 0 of warp w computes ratio w); one thread then forms the
+// β products and the weights from them.
+__device__ __forceinline__ double ens_abm_psi(const EnsCtl& c, double h, int j) {
+    return (j == 0) ? h : (j < c.k ? h + c.psi_prev[j - 1] : 1.0);
+}
+
+__device__ __forceinline__ void ens_abm_ratio(EnsCtl& c, double h, int w) {
+    if (w < 5) {
+        c.rat[w] = h * ens_rcp_in_range(ens_abm_psi(c, h, w));
+    } else {
+        const int i = w - 4;  // 1..4
+        c.rat[w] = (i < c.k) ? ens_abm_psi(c, h, i - 1) * ens_rcp_in_range(c.psi_prev[i - 1]) : 0.0;
+    }
+}
+
 __device__ __forceinline__ void ens_abm_coef(EnsCtl& c, double h) {
     const int k = c.k;
     c.kq = k;
     double psi[5], beta[5], r[5];
-    psi[0] = h;
 #pragma unroll
-    for (int i = 1; i < 5; ++i) psi[i] = (i < k) ? h + c.psi_prev[i - 1] : 1.0;
-#pragma unroll
-    for (int j = 0; j < 5; ++j) r[j] = h * ens_rcp_in_range(psi[j]);
+    for (int i = 0; i < 5; ++i) {
+        psi[i] = ens_abm_psi(c, h, i);
+        r[i] = c.rat[i];
+    }
     beta[0] = 1.0;
 #pragma unroll
-    for (int i = 1; i < 5; ++i) beta[i] = (i < k) ? beta[i - 1] * (psi[i - 1] * ens_rcp_in_range(c.psi_prev[i - 1])) : 0.0;
+    for (int i = 1; i < 5; ++i) beta[i] = (i < k) ? beta[i - 1] * c.rat[4 + i] : 0.0;
     double cq[8] = {0.0, 1.0, 1.0 / 2, 1.0 / 3, 1.0 / 4, 1.0 / 5, 1.0 / 6, 0.0};
 #pragma unroll
     for (int q = 1; q <= 6; ++q)
@@ -369,7 +386,7 @@ __device__ __forceinline__ void ens_abm_coef(EnsCtl& c, double h) {
 // the modified divided differences Phi_0..Phi_5 live in the stage buffers k[0..5], k[6] holds f at
 // the predicted and then at the corrected point)
 template <int BS, int ALG>
-__global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
+__global__ void __launch_bounds__(BS, 512 / BS) k_ensemble(EnsArgs A) {  // 128 registers a thread at any block size
     extern __shared__ __align__(16) float sm[];
     __shared__ double red[BS / 32];
     __shared__ EnsCtl c;
@@ -397,7 +414,8 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
     S.X = S.Z + (size_t)nq * m.P;
     S.tw = S.X + (size_t)m.nxi * H;
     S.pr = reinterpret_cast<double*>(S.tw + m.P / 2);
-    S.mb = reinterpret_cast<uint64_t*>(S.pr + 2 * (nch + 1));
+    S.cp = S.pr + 2 * (nch + 1);
+    S.mb = reinterpret_cast<uint64_t*>(S.cp + 3 * nch);
     S.xr = reinterpret_cast<float*>(S.mb + 4);
     S.G = m.ghat;
     if (A.gsm) {  // the spectra read every RHS: one copy per launch into shared memory
@@ -545,29 +563,30 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
             // with the error chunks; f at the corrected point and the Phi update after acceptance
             // every thread is done with the last step's beta (its Phi update) before thread 0 rewrites it
             __syncthreads();
+            if (lane == 0)
+                for (int w = warp; w < 9; w += BS / 32) ens_abm_ratio(c, dt, w);
+            __syncthreads();
             if (threadIdx.x == 0) ens_abm_coef(c, dt);
             __syncthreads();
             const int kq = c.kq;
             {
                 float* xb = S.xr + (size_t)(rx & 1) * N;
-                for (int i = lo + threadIdx.x; i < hi; i += BS) {
-                    double acc[3] = {0.0, 0.0, 0.0};
+                // one (component, patch) per thread: a CTA's slice of a split model is a few hundred
+                // elements, so its threads take the three components side by side instead of in turn
+                const int nl = hi - lo;
+                for (int t = threadIdx.x; t < 3 * nl; t += BS) {
+                    const int comp = (t >= nl) + (t >= 2 * nl);
+                    const int i = lo + t - comp * nl, g = comp * N + i;
+                    double acc = 0.0;
                     // compile-time bounds: the stage pointers stay in registers and every load of
                     // the differences issues before the first FMA needs one (same sums, same order)
 #pragma unroll
-                    for (int j = 0; j < 5; ++j) {
-                        if (j < kq) {
-                            const double bj = c.beta[j], gj = c.g[j];
-#pragma unroll
-                            for (int comp = 0; comp < 3; ++comp) acc[comp] = fma(gj, bj * kk[j][comp * N + i], acc[comp]);
-                        }
-                    }
-                    const double vnew = u[i] + dt * acc[0];
-                    y[i] = vnew;
-                    y[N + i] = u[N + i] + dt * acc[1];
-                    y[2 * N + i] = u[2 * N + i] + dt * acc[2];
-                    if (clus) {
-                        const float x = (float)(vnew - m.vpl);
+                    for (int j = 0; j < 5; ++j)
+                        if (j < kq) acc = fma(c.g[j], c.beta[j] * kk[j][g], acc);
+                    const double yv = u[g] + dt * acc;
+                    y[g] = yv;
+                    if (clus && comp == 0) {
+                        const float x = (float)(yv - m.vpl);
                         xb[i] = x;
                         for (int d = 1; d < csize; ++d) push_f32(xb + i, x, &S.mb[rx & 1], (rank + d) % csize);
                     }
@@ -579,41 +598,43 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
                 ens_rhs<BS>(m, A, S, y, kk[6], lo, hi, clus ? xb : nullptr);
                 ++rx;
             }
+            // corrector and error estimate, one warp per (chunk, component): each warp sums its 32
+            // patches' r^2 in a fixed shuffle order, and a chunk's norm is (s_v + s_θ) + s_δ, so a
+            // model's trajectory still does not depend on the block or cluster size
             const double gk = c.g[kq], ce = dt * (c.g[kq] - c.g[kq - 1]);
-            for (int ch = c0 + warp; ch < c1; ch += BS / 32) {
-                const int i = 32 * ch + lane;
+            const int ncp = 3 * (c1 - c0);
+            for (int wi = warp; wi < ncp; wi += BS / 32) {
+                const int q = wi / 3, comp = wi - 3 * q;
+                const int i = 32 * (c0 + q) + lane;
                 double ss = 0.0;
                 int bad = 0;
                 if (i < N) {
-                    double r[3];
+                    const int g = comp * N + i;
+                    double sacc = 0.0;
 #pragma unroll
-                    for (int comp = 0; comp < 3; ++comp) {
-                        const int g = comp * N + i;
-                        double sacc = 0.0;
-#pragma unroll
-                        for (int j = 0; j < 5; ++j)
-                            if (j < kq) sacc += c.beta[j] * kk[j][g];
-                        const double pk = kk[6][g] - sacc;
-                        const double yn = y[g] + dt * gk * pk;
-                        un[g] = yn;
-                        const double sc = (comp == 1 && m.log_theta) ? A.abstol + A.reltol
-                                                                     : A.abstol + A.reltol * fmax(fabs(u[g]), fabs(yn));
-                        r[comp] = (ce * pk) * ens_rcp_in_range(sc);
-                        bad |= !isfinite(yn);
-                    }
-                    ss = fma(r[0], r[0], ss);
-                    ss = fma(r[1], r[1], ss);
-                    ss = fma(r[2], r[2], ss);
+                    for (int j = 0; j < 5; ++j)
+                        if (j < kq) sacc += c.beta[j] * kk[j][g];
+                    const double pk = kk[6][g] - sacc;
+                    const double yn = y[g] + dt * gk * pk;
+                    un[g] = yn;
+                    const double sc = (comp == 1 && m.log_theta) ? A.abstol + A.reltol
+                                                                 : A.abstol + A.reltol * fmax(fabs(u[g]), fabs(yn));
+                    const double r = (ce * pk) * ens_rcp_in_range(sc);
+                    bad = !isfinite(yn);
+                    ss = r * r;
                 }
                 for (int o = 16; o > 0; o >>= 1) {
                     ss += __shfl_xor_sync(0xffffffffu, ss, o);
                     bad |= __shfl_xor_sync(0xffffffffu, bad, o);
                 }
-                if (lane == 0) {
-                    const double val = bad ? INFINITY : ss;
-                    prb[ch] = val;
-                    for (int d = 1; d < csize; ++d) push_f64(prb + ch, val, &S.mb[2 + e], (rank + d) % csize);
-                }
+                if (lane == 0) S.cp[wi] = bad ? INFINITY : ss;
+            }
+            __syncthreads();
+            for (int q = threadIdx.x; q < c1 - c0; q += BS) {
+                const int ch = c0 + q;
+                const double val = (S.cp[3 * q] + S.cp[3 * q + 1]) + S.cp[3 * q + 2];
+                prb[ch] = val;
+                for (int d = 1; d < csize; ++d) push_f64(prb + ch, val, &S.mb[2 + e], (rank + d) % csize);
             }
         }
         if (writer) {
@@ -741,9 +762,10 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
             const int kq = c.kq;
             // the old differences are loaded before any is overwritten (the stage buffers are
             // distinct arrays): one round trip instead of one per order, same arithmetic
-            for (int comp = 0; comp < 3; ++comp)
-                for (int i = lo + threadIdx.x; i < hi; i += BS) {
-                    const int g = comp * N + i;
+            const int nl = hi - lo;
+            for (int t = threadIdx.x; t < 3 * nl; t += BS) {  // one (component, patch) per thread
+                    const int comp = (t >= nl) + (t >= 2 * nl);
+                    const int g = comp * N + lo + t - comp * nl;
                     double old[5];
 #pragma unroll
                     for (int j = 0; j < 5; ++j) old[j] = (j < kq) ? kk[j][g] : 0.0;
@@ -775,11 +797,12 @@ __global__ void __launch_bounds__(BS) k_ensemble(EnsArgs A) {
 __global__ void k_ens_theta(EnsArgs A, int to_log);
 
 // FFT work arrays Z (nq x P), spectra X (nxi x H), twiddles (P/2), all float2; two buffers of
-// chunk norms + stop flag (doubles); four mbarriers; two slip-rate buffers of N floats
+// chunk norms + stop flag and the per-component chunk sums (doubles); four mbarriers; two
+// slip-rate buffers of N floats
 size_t ens_smem_bytes(int nx, int nxi, int P) {
     const size_t N = (size_t)nx * nxi, nch = (N + 31) / 32;
     return sizeof(float2) * ((size_t)((nxi + 1) / 2) * P + (size_t)nxi * (P / 2 + 1) + P / 2) +
-           sizeof(double) * 2 * (nch + 1) + sizeof(uint64_t) * 4 + sizeof(float) * 2 * N;
+           sizeof(double) * (2 * (nch + 1) + 3 * nch) + sizeof(uint64_t) * 4 + sizeof(float) * 2 * N;
 }
 
 int ens_prepare_model(EnsModel& m, int nx, int nxi, size_t* smem_bytes) {
@@ -915,7 +938,7 @@ int ens_max_clusters(int csize, int block, size_t smem, int alg) {
 bool ens_cluster16_ok(size_t smem, int alg) { return ens_max_clusters(16, 512, smem, alg) >= 1; }
 
 template <int BS>
-static int launch_cluster(const EnsArgs& A, int nmod, int csize, size_t smem, cudaStream_t s) {
+static int launch_cluster(const EnsArgs& A, int nmod, int csize, size_t smem, cudaStream_t s, int prioritize) {
     void (*kern)(EnsArgs) = (A.alg == 1) ? k_ensemble<BS, 1> : k_ensemble<BS, 0>;
     if (int rc = set_smem_limit((const void*)kern, (int)smem)) return rc;
     if (csize > 8)
@@ -930,7 +953,9 @@ static int launch_cluster(const EnsArgs& A, int nmod, int csize, size_t smem, cu
     at[0].val.clusterDim.x = (unsigned)csize;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
-    // larger clusters hold the stiffest models: their CTAs are dispatched first
+    // larger clusters hold the stiffest models: their CTAs are dispatched first (only where the
+    // ensemble has the GPU to itself; beside other work, such as a server's mantle requests on
+    // their own streams, the launches keep the default priority)
     int least = 0, greatest = 0;
     GBC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     int lg = 0;
@@ -938,14 +963,14 @@ static int launch_cluster(const EnsArgs& A, int nmod, int csize, size_t smem, cu
     at[1].id = cudaLaunchAttributePriority;
     at[1].val.priority = std::max(greatest, least - lg);
     cfg.attrs = at;
-    cfg.numAttrs = 2;
+    cfg.numAttrs = prioritize ? 2 : 1;
     GBC_CUDA(cudaLaunchKernelEx(&cfg, kern, A));
     return 0;
 }
 
 int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtmax, double dtmin,
                    unsigned long long budget_ns, int block, size_t smem, cudaStream_t main, int alg,
-                   size_t gbytes) {
+                   size_t gbytes, int prioritize) {
     EnsArgs A{};
     A.alg = alg;
     // Room for each CTA's copy of its model's spectra (the mixing then reads shared memory instead
@@ -971,9 +996,9 @@ int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtma
         A.gsm = gfit && (g > 0 || ctas <= sm_count()) ? 1 : 0;
         const size_t sg = A.gsm ? smem + gbytes + 16 : smem;
         int rc;
-        if (b == 128) rc = launch_cluster<128>(A, L.count[g], 1 << g, sg, s);
-        else if (b == 512) rc = launch_cluster<512>(A, L.count[g], 1 << g, sg, s);
-        else rc = launch_cluster<256>(A, L.count[g], 1 << g, sg, s);
+        if (b == 128) rc = launch_cluster<128>(A, L.count[g], 1 << g, sg, s, prioritize);
+        else if (b == 512) rc = launch_cluster<512>(A, L.count[g], 1 << g, sg, s, prioritize);
+        else rc = launch_cluster<256>(A, L.count[g], 1 << g, sg, s, prioritize);
         if (rc) return rc;
         GBC_CUDA(cudaEventRecord(L.join[g], s));
         GBC_CUDA(cudaStreamWaitEvent(main, L.join[g], 0));
@@ -1373,7 +1398,7 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
         int rc = 0;
         for (int k = 0; k < 2 && !rc; ++k)
             rc = ens_run_groups(e->lp, o->reltol, o->abstol, o->dtmax, o->dtmin, 100000000ull, b0, e->smem, s,
-                                o->alg, e->gbytes);
+                                o->alg, e->gbytes, 1);
         cudaError_t ce = cudaStreamEndCapture(s, &g);
         if (rc) return rc;
         GBC_CUDA(ce);
@@ -1426,7 +1451,7 @@ int gbc_ensemble_integrate_dev(gbc_ensemble* e, double* u_dev, const double* t0,
             return rc;
         for (;;) {
             if (int rc = ens_run_groups(e->lp, o->reltol, o->abstol, o->dtmax, o->dtmin, 100000000ull, block0(),
-                                        e->smem, s, o->alg, e->gbytes))
+                                        e->smem, s, o->alg, e->gbytes, 1))
                 return rc;
             GBC_CUDA(cudaMemcpyAsync(e->host.data(), e->d_models, sizeof(EnsModel) * e->n, cudaMemcpyDeviceToHost, s));
             GBC_CUDA(cudaStreamSynchronize(s));

@@ -79,7 +79,7 @@ int ens_launch_prepare(EnsLaunch& L, EnsModel* d_models, const EnsModel* host, i
 // itself and the spectra fit beside the FFT buffers, the launches stage them in shared memory
 int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtmax, double dtmin,
                    unsigned long long budget_ns, int block, size_t smem, cudaStream_t main, int alg = 0,
-                   size_t gbytes = 0);
+                   size_t gbytes = 0, int prioritize = 0);
 // θ <-> ln θ on the state of every descriptor with `logged` set
 int ens_theta(EnsModel* d_models, int n, int to_log, cudaStream_t s);
 void count_launches(long long n);
