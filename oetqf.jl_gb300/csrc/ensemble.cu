@@ -953,15 +953,14 @@ static int launch_cluster(const EnsArgs& A, int nmod, int csize, size_t smem, cu
     at[0].val.clusterDim.x = (unsigned)csize;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
-    // larger clusters hold the stiffest models: their CTAs are dispatched first (only where the
-    // ensemble has the GPU to itself; beside other work, such as a server's mantle requests on
-    // their own streams, the launches keep the default priority)
+    // prioritize 1: larger clusters hold the stiffest models, their CTAs are dispatched first;
+    // 2: every group at the greatest priority (a server's batch beside its mantle requests)
     int least = 0, greatest = 0;
     GBC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     int lg = 0;
     while ((1 << lg) < csize) ++lg;
     at[1].id = cudaLaunchAttributePriority;
-    at[1].val.priority = std::max(greatest, least - lg);
+    at[1].val.priority = (prioritize == 2) ? greatest : std::max(greatest, least - lg);
     cfg.attrs = at;
     cfg.numAttrs = prioritize ? 2 : 1;
     GBC_CUDA(cudaLaunchKernelEx(&cfg, kern, A));

@@ -77,6 +77,8 @@ int ens_launch_prepare(EnsLaunch& L, EnsModel* d_models, const EnsModel* host, i
 // one persistent launch per group: each model runs until done or budget_ns of wall clock
 // gbytes > 0: the largest model's spectra in bytes; when every CTA of the grouping gets an SM to
 // itself and the spectra fit beside the FFT buffers, the launches stage them in shared memory
+// prioritize: 0 default stream priority; 1 larger clusters at higher priority (the ensemble
+// alone on the GPU); 2 every group at the greatest priority (a server's batch beside other work)
 int ens_run_groups(const EnsLaunch& L, double reltol, double abstol, double dtmax, double dtmin,
                    unsigned long long budget_ns, int block, size_t smem, cudaStream_t main, int alg = 0,
                    size_t gbytes = 0, int prioritize = 0);

@@ -370,9 +370,13 @@ __global__ void k_gf_mm_expand(int ne, const int4* __restrict__ cell, int nX, in
 }
 
 // ---------------------------------------------------------------------------------------------
+// One item per thread: the CTAs are short-lived (an Okada evaluation each), so a multi-second
+// assembly does not hold the SMs for its whole duration and higher-priority work on other streams
+// (a server's batch and admissions) is dispatched as CTAs retire. The kernels keep their
+// grid-stride loops for grids beyond the launch limit.
 static int grid_for(long long total, int block) {
     long long g = (total + block - 1) / block;
-    long long cap = (long long)sm_count() * 32;
+    const long long cap = 0x7fffffffLL;
     if (g > cap) g = cap;
     return (int)(g < 1 ? 1 : g);
 }

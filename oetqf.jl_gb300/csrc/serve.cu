@@ -132,6 +132,14 @@ struct gbc_server {
     std::vector<std::unique_ptr<GfEntry>> cache;
     bool cache_on = true;
     long long hits = 0, misses = 0;
+    // evicted mantle models, destroyed by the reaper thread: freeing device memory waits for the
+    // device's queued work (another request's assembly can be seconds), which the scheduler thread
+    // must not do while it holds the lock or between batch iterations; the budget is a policy figure
+    // below the device's memory, so a free that lands a little later is safe
+    std::vector<gbc_model*> graveyard;
+    std::condition_variable reap_cv;
+    bool reap_stop = false;
+    std::thread reaper;
 
     double now() const {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
@@ -298,11 +306,29 @@ static void run_mantle(gbc_server* s, std::shared_ptr<Req> rp) {
     s->cv.notify_all();
 }
 
+// destroys evicted models outside the lock
+static void reaper(gbc_server* s) {
+    cudaSetDevice(0);
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+        s->reap_cv.wait(lk, [&] { return !s->graveyard.empty() || s->reap_stop; });
+        if (s->graveyard.empty()) break;  // stop requested and nothing left
+        std::vector<gbc_model*> g;
+        g.swap(s->graveyard);
+        lk.unlock();
+        for (gbc_model* m : g) gbc_model_destroy(m);
+        lk.lock();
+    }
+}
+
 // ---- scheduler ----------------------------------------------------------------------------------
 // the following hold s->mu
 static void drop_entry(gbc_server* s, GfEntry* e) {
     if (e->ghat) cudaFreeAsync(e->ghat, s->admit);
-    if (e->model) gbc_model_destroy(e->model);
+    if (e->model) {
+        s->graveyard.push_back(e->model);
+        s->reap_cv.notify_one();
+    }
     s->in_use -= e->bytes;
     for (size_t i = 0; i < s->cache.size(); ++i)
         if (s->cache[i].get() == e) { s->cache.erase(s->cache.begin() + i); break; }
@@ -445,7 +471,8 @@ static void scheduler(gbc_server* s) {
         if (!rc && cudaMemcpyAsync(s->d_desc, h.data(), sizeof(EnsModel) * n, cudaMemcpyHostToDevice, s->batch) != cudaSuccess) rc = GBC_ECUDA;
         if (!rc) rc = ens_launch_prepare(s->lp, s->d_desc, h.data(), n, 8, ens_boost(n), s->batch);
         if (!rc) rc = ens_run_groups(s->lp, s->batch_opts.reltol, s->batch_opts.abstol, s->batch_opts.dtmax,
-                                     s->batch_opts.dtmin, s->slice_ns, s->block, smem, s->batch, s->batch_opts.alg);
+                                     s->batch_opts.dtmin, s->slice_ns, s->block, smem, s->batch, s->batch_opts.alg,
+                                     0, 2);
         if (!rc && cudaMemcpyAsync(h.data(), s->d_desc, sizeof(EnsModel) * n, cudaMemcpyDeviceToHost, s->batch) != cudaSuccess) rc = GBC_ECUDA;
         if (!rc && cudaStreamSynchronize(s->batch) != cudaSuccess) rc = GBC_ECUDA;
         std::vector<std::shared_ptr<Req>> fin;
@@ -478,10 +505,21 @@ int gbc_server_create(double hbm_budget_bytes, const gbc_solver_opts* batch_opts
     s->budget = hbm_budget_bytes;
     s->batch_opts = *batch_opts;
     s->t_start = std::chrono::steady_clock::now();
-    cudaError_t e = cudaStreamCreateWithFlags(&s->batch, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->admit, cudaStreamNonBlocking);
+    // the scheduler's admission and batch work at the greatest stream priority: a mantle request's
+    // Green's-function assembly fills the GPU for seconds, and the scheduler thread waits for each
+    // admission; at a higher priority the small kernels are dispatched as the assembly's CTAs retire
+    int least = 0, greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->batch, cudaStreamNonBlocking, greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->admit, cudaStreamNonBlocking, greatest);
     if (e != cudaSuccess) { delete s; return cuda_fail(e, "cudaStreamCreate"); }
     if (int rc = upload_gl_tables()) { delete s; return rc; }
+    // batch descriptors for up to 1024 requests, allocated now: growing them later frees device
+    // memory on the scheduler thread, which waits for all queued work
+    s->d_desc_cap = 1024;
+    if (cudaMalloc(&s->d_desc, sizeof(EnsModel) * s->d_desc_cap) != cudaSuccess) { delete s; return fail(GBC_ENOMEM, "server batch descriptors"); }
+    if (int rc = ens_launch_create(s->lp, s->d_desc_cap)) { cudaFree(s->d_desc); delete s; return rc; }
+    s->reaper = std::thread(reaper, s);
     s->sched = std::thread(scheduler, s);
     *out = s;
     return 0;
@@ -595,7 +633,10 @@ void gbc_server_destroy(gbc_server* s) {
     {
         std::lock_guard<std::mutex> lk(s->mu);
         while (!s->cache.empty()) drop_entry(s, s->cache.back().get());
+        s->reap_stop = true;
+        s->reap_cv.notify_all();
     }
+    if (s->reaper.joinable()) s->reaper.join();
     if (s->d_desc) cudaFree(s->d_desc);
     ens_launch_destroy(s->lp);
     cudaStreamSynchronize(s->batch);
