@@ -334,8 +334,15 @@ static void drop_entry(gbc_server* s, GfEntry* e) {
         if (s->cache[i].get() == e) { s->cache.erase(s->cache.begin() + i); break; }
 }
 
-// evicts idle entries, least recently used first, until `need` more bytes fit; false if they cannot
+// evicts idle entries, least recently used first, until `need` more bytes fit; false if they cannot,
+// and then nothing is evicted (a request that cannot be admitted yet must not empty the cache on
+// every pass of the scheduler)
 static bool make_room(gbc_server* s, size_t need) {
+    if (s->in_use + need <= s->budget) return true;
+    size_t idle = 0;
+    for (auto& e : s->cache)
+        if (e->refs == 0) idle += e->bytes;
+    if (s->in_use + need > s->budget + idle) return false;
     while (s->in_use + need > s->budget) {
         GfEntry* victim = nullptr;
         for (auto& e : s->cache)

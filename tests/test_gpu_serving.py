@@ -120,3 +120,40 @@ def test_gf_cache_evicts_idle_geometries_under_budget():
     assert info.peak_bytes <= budget * 2**30
     assert info.cache_hits + info.cache_misses == 4
     assert info.cache_entries < info.cache_misses  # an idle geometry was evicted to admit a later one
+
+
+def _fault_bytes(cm):
+    """The server's charge for a fault-only request: its own buffers and its geometry's spectra."""
+    nx, nxi = cm.mf.nx, cm.mf.nξ
+    N, P = nx * nxi, 2
+    while P < 2 * nx - 1:
+        P *= 2
+    own = 8 * 37 * N + 4096
+    gf = 8 * (nx * nxi * nxi + 3 * nx + 4 * nxi) + 4 * nxi * nxi * (P // 2 + 1) + 512
+    return own, gf
+
+
+def test_waiting_request_does_not_empty_the_cache():
+    """A head request that cannot fit even with every idle geometry evicted must evict nothing: a
+    later request on a cached geometry, admitted around it, is a cache hit."""
+    import dataclasses
+    from oetqf_gb300.serving import Server
+    ms = fault_ensemble(n_models=6, years=0.05, n_range=(300, 420), seed=29)
+    ms = sorted(ms, key=lambda m: m.mf.nx)
+    a, b, c = ms[0], ms[2], ms[-1]  # 31 x 10, 36 x 10 and 41 x 10 patches
+    # steps of at most an hour: b (2 years, >= 17,520 steps) is still running while c and d arrive
+    b = dataclasses.replace(b, horizon=2 * YEAR)
+    own_a, gf_a = _fault_bytes(a)
+    own_b, gf_b = _fault_bytes(b)
+    own_c, gf_c = _fault_bytes(c)
+    budget = own_b + gf_b + own_c + gf_c - 1024  # b and c never run together
+    assert gf_a + own_b + gf_b + own_a <= budget  # a's geometry stays cached beside b, and d fits
+    s = Server(hbm_budget_gb=budget / 2**30, dtmax=3600.0)
+    _, ra = s.wait(s.submit(a))
+    ib, ic, idd = s.submit(b), s.submit(c), s.submit(dataclasses.replace(a))
+    rb, rc, rd = [s.wait(i)[1] for i in (ib, ic, idd)]
+    info = s.info()
+    s.close()
+    assert all(r.status == 0 for r in (ra, rb, rc, rd))
+    assert rd.admit_s < rc.admit_s and rc.admit_s >= rb.done_s  # c waited for b; d went around it
+    assert (info.cache_hits, info.cache_misses) == (1, 3)
