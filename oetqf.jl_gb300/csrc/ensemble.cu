@@ -115,25 +115,28 @@ __device__ __forceinline__ double ens_rcp_in_range(double x) {
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 
-// in-place radix-2 DIT FFT of nq arrays of length P already in bit-reversed order; forward uses
-// twiddles e^{-2πi t/P}, inverse their conjugates (no scaling). Two consecutive radix-2 stages are
-// done per pass with a thread's four elements in registers (the same operations in the same
-// order), so a pass needs one barrier instead of two.
 __device__ __forceinline__ float2 bfly_add(float2 a, float2 c) { return make_float2(a.x + c.x, a.y + c.y); }
 __device__ __forceinline__ float2 bfly_sub(float2 a, float2 c) { return make_float2(a.x - c.x, a.y - c.y); }
+// Shared-memory FFT buffers (work arrays and twiddles) hold element i at i + i / 8: one float2 of
+// padding per eight. The strided accesses of the radix-8 passes (stride 8 in the first) and the
+// bit-reversed scatters then spread over the 32 banks instead of landing on two.
+__device__ __forceinline__ int zp(int i) { return i + (i >> 3); }
+__host__ __device__ __forceinline__ size_t zlen(size_t n) { return n + (n >> 3) + 1; }
+
 __device__ __forceinline__ float2 tw_get(const float2* tw, int idx, int inverse) {
-    float2 w = tw[idx];
+    float2 w = tw[zp(idx)];
     if (inverse) w.y = -w.y;
     return w;
 }
 
-// in-place radix-2 DIT FFT of nq arrays of length P (P = 2^logP) already in bit-reversed order;
-// forward uses twiddles e^{-2πi t/P}, inverse their conjugates (no scaling). Up to three
+// in-place radix-2 DIT FFT of arrays q0 .. q0 + nq - 1 (length P = 2^logP, padded as above) of the
+// buffer Z, already in bit-reversed order; forward uses twiddles e^{-2πi t/P}, inverse their
+// conjugates (no scaling). Up to three
 // consecutive radix-2 stages are done per pass with a thread's eight elements in registers (the
 // same butterflies in the same order as one stage per pass), so a 512-point transform takes three
 // passes and barriers; indices come from shifts (P is a power of two).
 template <int BS>
-__device__ __forceinline__ void fft_many(float2* Z, int nq, int P, int logP, const float2* tw, int inverse) {
+__device__ __forceinline__ void fft_many(float2* Z, int q0, int nq, int P, int logP, const float2* tw, int inverse) {
     int st = 0;
     while (st < logP) {
         const int ns = min(3, logP - st);       // stages in this pass
@@ -143,12 +146,12 @@ __device__ __forceinline__ void fft_many(float2* Z, int nq, int P, int logP, con
         for (int t = threadIdx.x; t < items; t += BS) {
             const int q = t >> lgi, r = t & ((1 << lgi) - 1);
             const int g = r >> st, pos = r & (h - 1);
-            float2* z = Z + (size_t)q * P;
+            const int zb = (q0 + q) * P;  // arrays q0.. of the padded buffer
             if (ns == 3) {
                 const int b0 = g * 8 * h + pos;
                 float2 x[8];
 #pragma unroll
-                for (int m = 0; m < 8; ++m) x[m] = z[b0 + m * h];
+                for (int m = 0; m < 8; ++m) x[m] = Z[zp(zb + b0 + m * h)];
                 const float2 w1 = tw_get(tw, pos * (P >> (st + 1)), inverse);
 #pragma unroll
                 for (int m = 0; m < 8; m += 2) {  // stage st: pairs (m, m+1)
@@ -172,29 +175,29 @@ __device__ __forceinline__ void fft_many(float2* Z, int nq, int P, int logP, con
                     x[m] = bfly_add(x[m], c);
                 }
 #pragma unroll
-                for (int m = 0; m < 8; ++m) z[b0 + m * h] = x[m];
+                for (int m = 0; m < 8; ++m) Z[zp(zb + b0 + m * h)] = x[m];
             } else if (ns == 2) {
                 const int b0 = g * 4 * h + pos;
                 const float2 w1 = tw_get(tw, pos * (P >> (st + 1)), inverse);
                 const float2 w2a = tw_get(tw, pos * (P >> (st + 2)), inverse);
                 const float2 w2b = tw_get(tw, (pos + h) * (P >> (st + 2)), inverse);
-                const float2 x0 = z[b0], x1 = z[b0 + h], x2 = z[b0 + 2 * h], x3 = z[b0 + 3 * h];
+                const float2 x0 = Z[zp(zb + b0)], x1 = Z[zp(zb + b0 + h)], x2 = Z[zp(zb + b0 + 2 * h)], x3 = Z[zp(zb + b0 + 3 * h)];
                 float2 c = cmul(x1, w1);
                 const float2 y0 = bfly_add(x0, c), y1 = bfly_sub(x0, c);
                 c = cmul(x3, w1);
                 const float2 y2 = bfly_add(x2, c), y3 = bfly_sub(x2, c);
                 c = cmul(y2, w2a);
-                z[b0] = bfly_add(y0, c);
-                z[b0 + 2 * h] = bfly_sub(y0, c);
+                Z[zp(zb + b0)] = bfly_add(y0, c);
+                Z[zp(zb + b0 + 2 * h)] = bfly_sub(y0, c);
                 c = cmul(y3, w2b);
-                z[b0 + h] = bfly_add(y1, c);
-                z[b0 + 3 * h] = bfly_sub(y1, c);
+                Z[zp(zb + b0 + h)] = bfly_add(y1, c);
+                Z[zp(zb + b0 + 3 * h)] = bfly_sub(y1, c);
             } else {
                 const int i0 = (g << (st + 1)) + pos, i1 = i0 + h;
                 const float2 w = tw_get(tw, pos * (P >> (st + 1)), inverse);
-                const float2 a = z[i0], c = cmul(z[i1], w);
-                z[i0] = bfly_add(a, c);
-                z[i1] = bfly_sub(a, c);
+                const float2 a = Z[zp(zb + i0)], c = cmul(Z[zp(zb + i1)], w);
+                Z[zp(zb + i0)] = bfly_add(a, c);
+                Z[zp(zb + i1)] = bfly_sub(a, c);
             }
         }
         st += ns;
@@ -230,14 +233,14 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
                 if (2 * q + 1 < nxi) im = (float)(v[i + nx * (2 * q + 1)] - m.vpl);
             }
         }
-        S.Z[q * P + (__brev(i) >> (32 - logP))] = make_float2(re, im);
+        S.Z[zp(q * P + (__brev(i) >> (32 - logP)))] = make_float2(re, im);
     }
     __syncthreads();
-    fft_many<BS>(S.Z, nq, P, logP, S.tw, 0);
+    fft_many<BS>(S.Z, 0, nq, P, logP, S.tw, 0);
     // separate the two real spectra: X_{2q}[f] = (Z[f] + conj Z[P-f]) / 2, X_{2q+1} = (Z[f] - conj Z[P-f]) / 2i
     for (int t = threadIdx.x; t < nq * H; t += BS) {
         const int q = t / H, f = t - q * H;
-        const float2 a = S.Z[q * P + f], b = S.Z[q * P + ((P - f) & (P - 1))];
+        const float2 a = S.Z[zp(q * P + f)], b = S.Z[zp(q * P + ((P - f) & (P - 1)))];
         S.X[(2 * q) * H + f] = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
         if (2 * q + 1 < nxi) S.X[(2 * q + 1) * H + f] = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
     }
@@ -267,12 +270,11 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
             }
         }
         // W[f] = Y0[f] + i Y1[f]; W[P-f] = conj(Y0[f]) + i conj(Y1[f])
-        float2* W = S.Z + q * P;
-        W[__brev(f) >> (32 - logP)] = make_float2(y0.x - y1.y, y0.y + y1.x);
-        if (f > 0 && f < P - f) W[__brev(P - f) >> (32 - logP)] = make_float2(y0.x + y1.y, -y0.y + y1.x);
+        S.Z[zp(q * P + (__brev(f) >> (32 - logP)))] = make_float2(y0.x - y1.y, y0.y + y1.x);
+        if (f > 0 && f < P - f) S.Z[zp(q * P + (__brev(P - f) >> (32 - logP)))] = make_float2(y0.x + y1.y, -y0.y + y1.x);
     }
     __syncthreads();
-    fft_many<BS>(S.Z + (size_t)qlo * P, nqr, P, logP, S.tw, 1);
+    fft_many<BS>(S.Z, qlo, nqr, P, logP, S.tw, 1);
     const double invP = 1.0 / P;
     const double* pa = m.a;
     const double* pb = m.b;
@@ -281,7 +283,7 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
     const double* pc = m.c1;
     for (int i = lo + threadIdx.x; i < hi; i += BS) {
         const int ii = i % nx, j = i / nx;
-        const float2 w = S.Z[(j >> 1) * P + ii];
+        const float2 w = S.Z[zp((j >> 1) * P + ii)];
         const double dtau = (double)((j & 1) ? w.y : w.x) * invP;
         const double vi = v[i];
         const double ai = pa[i], bi = pb[i], Li = pL[i];
@@ -411,9 +413,9 @@ __global__ void __launch_bounds__(BS, 512 / BS) k_ensemble(EnsArgs A) {  // 128 
     const bool clus = csize > 1;
     EnsSmem S;
     S.Z = reinterpret_cast<float2*>(sm);
-    S.X = S.Z + (size_t)nq * m.P;
+    S.X = S.Z + zlen((size_t)nq * m.P);
     S.tw = S.X + (size_t)m.nxi * H;
-    S.pr = reinterpret_cast<double*>(S.tw + m.P / 2);
+    S.pr = reinterpret_cast<double*>(S.tw + zlen((size_t)m.P / 2));
     S.cp = S.pr + 2 * (nch + 1);
     S.mb = reinterpret_cast<uint64_t*>(S.cp + 3 * nch);
     S.xr = reinterpret_cast<float*>(S.mb + 4);
@@ -428,7 +430,7 @@ __global__ void __launch_bounds__(BS, 512 / BS) k_ensemble(EnsArgs A) {  // 128 
     for (int t = threadIdx.x; t < m.P / 2; t += BS) {
         double sn, cs;
         sincospi(2.0 * t / m.P, &sn, &cs);
-        S.tw[t] = make_float2((float)cs, (float)-sn);
+        S.tw[zp(t)] = make_float2((float)cs, (float)-sn);
     }
     __shared__ int xfail;  // a bounded exchange wait gave up
     if (threadIdx.x == 0) {
@@ -796,12 +798,12 @@ __global__ void __launch_bounds__(BS, 512 / BS) k_ensemble(EnsArgs A) {  // 128 
 
 __global__ void k_ens_theta(EnsArgs A, int to_log);
 
-// FFT work arrays Z (nq x P), spectra X (nxi x H), twiddles (P/2), all float2; two buffers of
+// FFT work arrays Z (nq x P, padded), spectra X (nxi x H), twiddles (P/2, padded), all float2; two buffers of
 // chunk norms + stop flag and the per-component chunk sums (doubles); four mbarriers; two
 // slip-rate buffers of N floats
 size_t ens_smem_bytes(int nx, int nxi, int P) {
     const size_t N = (size_t)nx * nxi, nch = (N + 31) / 32;
-    return sizeof(float2) * ((size_t)((nxi + 1) / 2) * P + (size_t)nxi * (P / 2 + 1) + P / 2) +
+    return sizeof(float2) * (zlen((size_t)((nxi + 1) / 2) * P) + (size_t)nxi * (P / 2 + 1) + zlen((size_t)P / 2)) +
            sizeof(double) * (2 * (nch + 1) + 3 * nch) + sizeof(uint64_t) * 4 + sizeof(float) * 2 * N;
 }
 
