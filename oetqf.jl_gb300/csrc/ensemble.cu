@@ -93,20 +93,13 @@ __device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, unsigned parity
 }
 
 // 1/x by Newton-Raphson (r <- r + r (1 - x r), the relative error squaring each step) from the
-// correctly rounded FP32 reciprocal of x rounded to FP32 (error < 2^-23): two steps leave ~2^-90
-// plus FP64 rounding, about 1 ulp -- four dependent FMAs where an FP64 division is a long chain of
-// dependent FP64 instructions at 64 cycles each on this chip. Outside FP32's normal range the
-// seed is not usable and the plain division runs.
-__device__ __forceinline__ double ens_rcp(double x) {
-    const double ax = fabs(x);
-    if (!(ax > 1e-36 && ax < 1e36)) return 1.0 / x;
-    double r = (double)__frcp_rn(__double2float_rn(x));
-    r = fma(r, fma(-x, r, 1.0), r);
-    return fma(r, fma(-x, r, 1.0), r);
-}
-
-// The same reciprocal without the range check, for arguments known to lie in FP32's normal range
-// (step sizes, error-norm scales, friction denominators): three FP64 instructions fewer.
+// FP64 reciprocal by Newton-Raphson from the correctly rounded FP32 reciprocal of x rounded to FP32
+// (error < 2^-23): two steps leave ~2^-90 plus FP64 rounding, about 1 ulp -- four dependent FMAs
+// where an FP64 division is a long chain of dependent FP64 instructions at 64 cycles each on this
+// chip. For arguments in FP32's normal range: step sizes, error-norm scales, the state θ (between
+// about 1e-3 and 1e12 s over a cycle) and friction denominators (at least the radiation damping
+// η). Below that range the seed overflows and the result is not finite (the step control rejects
+// the stage); above it the result is zero.
 __device__ __forceinline__ double ens_rcp_in_range(double x) {
     double r = (double)__frcp_rn(__double2float_rn(x));
     r = fma(r, fma(-x, r, 1.0), r);
@@ -307,7 +300,7 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
             const double vp = vi * psi1;
             const double psi2 = ps[i] * psi1 * rsqrt(fma(vp, vp, 1.0));
             const double dth = fma(-vi * tht, m.iL[i], 1.0);
-            k[i] = fma(-bi * vi * psi2, dth * ens_rcp(tht), dtau) * ens_rcp_in_range(fma(ai, psi2, m.eta));
+            k[i] = fma(-bi * vi * psi2, dth * ens_rcp_in_range(tht), dtau) * ens_rcp_in_range(fma(ai, psi2, m.eta));
             k[N + i] = dth;
         }
         k[2 * N + i] = vi;
