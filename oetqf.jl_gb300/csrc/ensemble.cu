@@ -52,7 +52,7 @@ __constant__ double e_te[7] = {-0.00178001105222577714, -0.0008164344596567469, 
 // spectra X (nxi x H complex), twiddles (P/2 complex).
 struct EnsSmem {
     float2* Z;
-    float2* X;
+    float2* W;      // mixed row pairs of the CTA's patches, inverse-transformed in place (padded)
     float2* tw;
     double* pr;     // 2 x (nch + 1): error-norm sums of every 32-patch chunk + rank 0's stop flag
     double* cp;     // 3 x nch: VCABM5 error-norm sums of the CTA's chunks, one per component
@@ -230,44 +230,46 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
     }
     __syncthreads();
     fft_many<BS>(S.Z, 0, nq, P, logP, S.tw, 0);
-    // separate the two real spectra: X_{2q}[f] = (Z[f] + conj Z[P-f]) / 2, X_{2q+1} = (Z[f] - conj Z[P-f]) / 2i
-    for (int t = threadIdx.x; t < nq * H; t += BS) {
-        const int q = t / H, f = t - q * H;
-        const float2 a = S.Z[zp(q * P + f)], b = S.Z[zp(q * P + ((P - f) & (P - 1)))];
-        S.X[(2 * q) * H + f] = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
-        if (2 * q + 1 < nxi) S.X[(2 * q + 1) * H + f] = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
-    }
-    __syncthreads();
-    // Y_j[f] = sum_l G[j,l,f] X_l[f] (G real); repack (2q, 2q+1) as Y_2q + i Y_2q+1 with Hermitian fill,
-    // bit-reversed for the inverse transform. Only the row pairs holding this CTA's patches [lo, hi)
-    // are mixed and transformed back (a cluster rank's slice spans one or two depth rows): the
-    // forward spectra of every row are needed, the traction rates of the other rows are not.
+    // Y_j[f] = sum_l G[j,l,f] X_l[f] (G real), the row spectra X taken straight from the transformed
+    // pairs: X_{2q}[f] = (Z_q[f] + conj Z_q[P-f]) / 2, X_{2q+1}[f] = (Z_q[f] - conj Z_q[P-f]) / 2i.
+    // Y is repacked (2q, 2q+1) as Y_2q + i Y_2q+1 with Hermitian fill, bit-reversed, into W for the
+    // inverse transform (every thread still reads Z). Only the row pairs holding this CTA's patches
+    // [lo, hi) are mixed and transformed back (a cluster rank's slice spans one or two depth rows):
+    // the forward spectra of every row are needed, the traction rates of the other rows are not.
     const float* G = S.G;
     const int qlo = (hi > lo) ? (lo / nx) >> 1 : 0;
     const int nqr = (hi > lo) ? (((hi - 1) / nx) >> 1) - qlo + 1 : 0;
     for (int t = threadIdx.x; t < nqr * H; t += BS) {
-        const int q = qlo + t / H, f = t - (q - qlo) * H;
+        const int q = qlo + t / H, f = t - (q - qlo) * H, fm = (P - f) & (P - 1);
         const int j0 = 2 * q, j1 = 2 * q + 1;
         float2 y0 = make_float2(0.f, 0.f), y1 = make_float2(0.f, 0.f);
-        for (int l = 0; l < nxi; ++l) {
-            const float2 x = S.X[l * H + f];
-            // generic loads: G is global memory or a shared-memory copy (a read-only-path load
-            // would accept only global addresses)
-            const float g0 = G[((size_t)(j0 * nxi + l)) * H + f];
-            y0.x = fmaf(g0, x.x, y0.x);
-            y0.y = fmaf(g0, x.y, y0.y);
-            if (j1 < nxi) {
-                const float g1 = G[((size_t)(j1 * nxi + l)) * H + f];
-                y1.x = fmaf(g1, x.x, y1.x);
-                y1.y = fmaf(g1, x.y, y1.y);
+        for (int qi = 0; qi < nq; ++qi) {
+            const float2 a = S.Z[zp(qi * P + f)], b = S.Z[zp(qi * P + fm)];
+#pragma unroll
+            for (int s2 = 0; s2 < 2; ++s2) {
+                const int l = 2 * qi + s2;
+                if (l >= nxi) break;
+                const float2 x = s2 ? make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x))
+                                    : make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+                // generic loads: G is global memory or a shared-memory copy (a read-only-path load
+                // would accept only global addresses)
+                const float g0 = G[((size_t)(j0 * nxi + l)) * H + f];
+                y0.x = fmaf(g0, x.x, y0.x);
+                y0.y = fmaf(g0, x.y, y0.y);
+                if (j1 < nxi) {
+                    const float g1 = G[((size_t)(j1 * nxi + l)) * H + f];
+                    y1.x = fmaf(g1, x.x, y1.x);
+                    y1.y = fmaf(g1, x.y, y1.y);
+                }
             }
         }
         // W[f] = Y0[f] + i Y1[f]; W[P-f] = conj(Y0[f]) + i conj(Y1[f])
-        S.Z[zp(q * P + (__brev(f) >> (32 - logP)))] = make_float2(y0.x - y1.y, y0.y + y1.x);
-        if (f > 0 && f < P - f) S.Z[zp(q * P + (__brev(P - f) >> (32 - logP)))] = make_float2(y0.x + y1.y, -y0.y + y1.x);
+        const int wb = (q - qlo) * P;
+        S.W[zp(wb + (__brev(f) >> (32 - logP)))] = make_float2(y0.x - y1.y, y0.y + y1.x);
+        if (f > 0 && f < P - f) S.W[zp(wb + (__brev(P - f) >> (32 - logP)))] = make_float2(y0.x + y1.y, -y0.y + y1.x);
     }
     __syncthreads();
-    fft_many<BS>(S.Z, qlo, nqr, P, logP, S.tw, 1);
+    fft_many<BS>(S.W, 0, nqr, P, logP, S.tw, 1);
     const double invP = 1.0 / P;
     const double* pa = m.a;
     const double* pb = m.b;
@@ -276,7 +278,7 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
     const double* pc = m.c1;
     for (int i = lo + threadIdx.x; i < hi; i += BS) {
         const int ii = i % nx, j = i / nx;
-        const float2 w = S.Z[zp((j >> 1) * P + ii)];
+        const float2 w = S.W[zp(((j >> 1) - qlo) * P + ii)];
         const double dtau = (double)((j & 1) ? w.y : w.x) * invP;
         const double vi = v[i];
         const double ai = pa[i], bi = pb[i], Li = pL[i];
@@ -401,13 +403,13 @@ __global__ void __launch_bounds__(BS, 512 / BS) k_ensemble(EnsArgs A) {  // 128 
     const double inv3n = 1.0 / (double)(3 * N);  // the RMS error norm's 1/n, once per launch
     const int lo = 32 * (int)((long long)nch * rank / csize);
     const int hi = min(N, 32 * (int)((long long)nch * (rank + 1) / csize));
-    const int nq = (m.nxi + 1) / 2, H = m.P / 2 + 1;
+    const int nq = (m.nxi + 1) / 2;
     const int c0 = (int)((long long)nch * rank / csize), c1 = (int)((long long)nch * (rank + 1) / csize);
     const bool clus = csize > 1;
     EnsSmem S;
     S.Z = reinterpret_cast<float2*>(sm);
-    S.X = S.Z + zlen((size_t)nq * m.P);
-    S.tw = S.X + (size_t)m.nxi * H;
+    S.W = S.Z + zlen((size_t)nq * m.P);
+    S.tw = S.W + zlen((size_t)nq * m.P);
     S.pr = reinterpret_cast<double*>(S.tw + zlen((size_t)m.P / 2));
     S.cp = S.pr + 2 * (nch + 1);
     S.mb = reinterpret_cast<uint64_t*>(S.cp + 3 * nch);
@@ -791,12 +793,12 @@ __global__ void __launch_bounds__(BS, 512 / BS) k_ensemble(EnsArgs A) {  // 128 
 
 __global__ void k_ens_theta(EnsArgs A, int to_log);
 
-// FFT work arrays Z (nq x P, padded), spectra X (nxi x H), twiddles (P/2, padded), all float2; two buffers of
+// FFT work arrays Z and W (nq x P each, padded), twiddles (P/2, padded), all float2; two buffers of
 // chunk norms + stop flag and the per-component chunk sums (doubles); four mbarriers; two
 // slip-rate buffers of N floats
 size_t ens_smem_bytes(int nx, int nxi, int P) {
     const size_t N = (size_t)nx * nxi, nch = (N + 31) / 32;
-    return sizeof(float2) * (zlen((size_t)((nxi + 1) / 2) * P) + (size_t)nxi * (P / 2 + 1) + zlen((size_t)P / 2)) +
+    return sizeof(float2) * (2 * zlen((size_t)((nxi + 1) / 2) * P) + zlen((size_t)P / 2)) +
            sizeof(double) * (2 * (nch + 1) + 3 * nch) + sizeof(uint64_t) * 4 + sizeof(float) * 2 * N;
 }
 
