@@ -282,25 +282,27 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
         const double dtau = (double)((j & 1) ? w.y : w.x) * invP;
         const double vi = v[i];
         const double ai = pa[i], bi = pb[i], Li = pL[i];
+        // ψ1 = exp((f0 + b ln(v0 θ / L)) / a) / (2 v0) = exp(c1 + (b/a) ln θ) and ψ2 = σ ψ1 / hypot(1, v ψ1)
+        // = σ / sqrt(v² + ψ1⁻²). ψ1⁻¹ is tiny against the slip rate (ψ1⁻¹ ≲ 1e-9 m/s and ψ1⁻¹ / v ≲
+        // 1e-4 over a cycle: ψ1 grows with θ as v falls), so it enters ψ2 only as a correction of
+        // relative size ψ1⁻² / v²; computed with FP32 exp and log it moves ψ2 by ≲ 1e-13 relative, and
+        // its ~40 FP64 instructions (a warp issues one per 64 cycles) become FP32 ones. The rest of the
+        // friction is FP64; the per-patch constants replace three serial divisions.
         if (m.log_theta) {
-            // ψ = ln θ: ψ1 = exp(c1 + (b/a) ψ), 1/θ = exp(-ψ); dψ = 1/θ - v/L; dμ/dθ dθ = b v ψ2 dψ;
-            // ψ2 = σ ψ1 / hypot(1, v ψ1) as one reciprocal square root
+            // ψ = ln θ: 1/θ = exp(-ψ) (FP64: the ageing law's 1/θ - v/L cancels near steady state);
+            // dψ = 1/θ - v/L; dμ/dθ dθ = b v ψ2 dψ
             const double psi = th[i];
-            const double psi1 = exp(fma(m.boa[i], psi, pc[i]));
-            const double vp = vi * psi1;
-            const double psi2 = ps[i] * psi1 * rsqrt(fma(vp, vp, 1.0));
+            const double ei = (double)expf(-fmaf(__double2float_rn(m.boa[i]), __double2float_rn(psi), __double2float_rn(pc[i])));
+            const double psi2 = ps[i] * rsqrt(fma(vi, vi, ei * ei));
             const double dpsi = fma(-vi, m.iL[i], exp(-psi));
             k[i] = fma(-bi * vi * psi2, dpsi, dtau) / fma(ai, psi2, m.eta);
             k[N + i] = dpsi;
         } else {
-            // ψ1 = exp((f0 + b ln(v0 θ / L)) / a) / (2 v0) = exp(c1 + (b/a) ln θ), ψ2 = σ ψ1 / hypot(1, v ψ1)
-            // as one reciprocal square root; the per-patch constants replace three serial divisions
-            // (each FP64 step of this chain costs a warp 64 cycles on this chip)
             const double tht = th[i];
             (void)Li;
-            const double psi1 = exp(fma(m.boa[i], log(fmax(0.0, tht)), pc[i]));
-            const double vp = vi * psi1;
-            const double psi2 = ps[i] * psi1 * rsqrt(fma(vp, vp, 1.0));
+            const float lt = logf(fmaxf(0.f, __double2float_rn(tht)));  // θ <= 0: ψ1 = 0, ψ2 = 0
+            const double ei = (double)expf(-fmaf(__double2float_rn(m.boa[i]), lt, __double2float_rn(pc[i])));
+            const double psi2 = ps[i] * rsqrt(fma(vi, vi, ei * ei));
             const double dth = fma(-vi * tht, m.iL[i], 1.0);
             k[i] = fma(-bi * vi * psi2, dth * ens_rcp_in_range(tht), dtau) * ens_rcp_in_range(fma(ai, psi2, m.eta));
             k[N + i] = dth;
