@@ -1146,14 +1146,14 @@ int gbc_ensemble_create(int nmodels, const int* nx, const int* nxi, gbc_ensemble
             return fail(GBC_EINVAL, "ensemble model sizes must satisfy 0 < nx <= 4096, 0 < nxi <= 64");
         }
         EnsModel& m = e->host[i];
-        memset(&m, 0, sizeof(m));
-        m.nx = nx[i]; m.nxi = nxi[i]; m.N = nx[i] * nxi[i];
-        m.P = 2; m.logP = 1;
-        while (m.P < 2 * nx[i] - 1) { m.P <<= 1; ++m.logP; }
+        size_t sm = 0;
+        if (int rc = ens_prepare_model(m, nx[i], nxi[i], &sm)) {  // sizes and FFT length, as the server's
+            delete e;
+            return rc;
+        }
         m.off_n = on; m.off_st = os;
         on += m.N;
         os += (long long)nxi[i] * nxi[i] * (m.P / 2 + 1);
-        const size_t sm = ens_smem_bytes(nx[i], nxi[i], m.P);
         e->smem = std::max(e->smem, sm);
         e->gbytes = std::max(e->gbytes, sizeof(float) * ens_ghat_floats(m));
     }
