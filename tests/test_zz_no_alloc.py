@@ -97,3 +97,62 @@ def test_noalloc_matches_regular_rhs_twice(oracle):
         ref = m.rhs_flat(u)
         assert np.all(np.isfinite(got))
         np.testing.assert_allclose(got, ref, rtol=RTOL, atol=1e-12 * np.abs(ref).max())
+
+
+@pytest.mark.gpu
+def test_noalloc_replays_from_a_cuda_graph(oracle):
+    """The call recorded into a CUDA graph (torch.cuda.graph, global capture mode: an allocation or a
+    device-wide synchronisation anywhere in the process would fail the capture) and replayed with
+    new states copied into the same buffer: each replay equals the regular entry point."""
+    torch = pytest.importorskip("torch")
+    from oetqf_gb300 import _capi as C
+    from oetqf_gb300.equation import GB300Model
+    mf, ma, st, g12, g21, g22, pf, pa = _model(oracle)
+    N, ne = mf.nx * mf.nξ, ma.ne
+    M = 6 * ne
+    m = GB300Model(mf.nx, mf.nξ, ne)
+    m.set_gf(C.GBC_GF11_REAL, st)
+    m.set_gf(C.GBC_GF12, g12)
+    m.set_gf(C.GBC_GF21, g21)
+    m.set_gf(C.GBC_GF22, g22)
+    m.set_fault_props(pf)
+    m.set_mantle_props(pa)
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a, dtype=np.float64).reshape(-1), device="cuda:0")
+    npad = (N + 31) // 32 * 32
+    ldm = npad + M
+    gm = np.zeros((M, ldm))
+    gm[:, :N], gm[:, npad:npad + M] = g12, g22
+    d_st, d_gm, d_g21 = dev(st.reshape(-1, order="F")), dev(gm), dev(g21)
+    d_a, d_b, d_L, d_s = (dev(q.reshape(-1, order="F")) for q in (pf.a, pf.b, pf.L, pf.σ))
+    d_gam, d_n = dev(pa.γ), dev(pa.n)
+    deps0 = np.ascontiguousarray(pa.dϵ0)
+    d_u = torch.zeros(m.state_len, dtype=torch.float64, device="cuda:0")
+    d_du = torch.zeros(m.state_len, dtype=torch.float64, device="cuda:0")
+
+    def call():
+        return C.lib().gbc_rhs_visco_noalloc(
+            mf.nx, mf.nξ, ne, d_st.data_ptr(), d_gm.data_ptr(), ldm, d_g21.data_ptr(), M, d_a.data_ptr(),
+            d_b.data_ptr(), d_L.data_ptr(), d_s.data_ptr(), pf.η, pf.vpl, pf.f0, pf.v0, d_gam.data_ptr(),
+            d_n.data_ptr(), C.ptr(deps0), d_u.data_ptr(), d_du.data_ptr(),
+            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+
+    rng = np.random.default_rng(23)
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):  # one call outside the capture (kernels loaded, scratch address cached)
+        d_u.copy_(dev(rng.random(m.state_len)))
+        C.check(call())
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        rc = call()
+    C.check(rc)
+    for _ in range(2):
+        u = rng.random(m.state_len)
+        d_u.copy_(dev(u))
+        d_du.fill_(float("nan"))
+        g.replay()
+        torch.cuda.synchronize()
+        got = d_du.cpu().numpy()
+        ref = m.rhs_flat(u)
+        assert np.all(np.isfinite(got))
+        np.testing.assert_allclose(got, ref, rtol=RTOL, atol=1e-12 * np.abs(ref).max())
