@@ -146,13 +146,17 @@ def test_noalloc_replays_from_a_cuda_graph(oracle):
     with torch.cuda.graph(g):
         rc = call()
     C.check(rc)
+    sentinel = 1.25e300  # every entry of du is written by the replay
     for _ in range(2):
         u = rng.random(m.state_len)
         d_u.copy_(dev(u))
-        d_du.fill_(float("nan"))
+        d_du.fill_(sentinel)
         g.replay()
         torch.cuda.synchronize()
         got = d_du.cpu().numpy()
         ref = m.rhs_flat(u)
-        assert np.all(np.isfinite(got))
-        np.testing.assert_allclose(got, ref, rtol=RTOL, atol=1e-12 * np.abs(ref).max())
+        assert not np.any(got == sentinel)
+        # the random friction properties can overflow ψ1 on a patch: the same non-finite entries
+        np.testing.assert_array_equal(np.isfinite(got), np.isfinite(ref))
+        fin = np.isfinite(ref)
+        np.testing.assert_allclose(got[fin], ref[fin], rtol=RTOL, atol=1e-12 * np.abs(ref[fin]).max())
