@@ -128,9 +128,37 @@ __device__ __forceinline__ float2 tw_get(const float2* tw, int idx, int inverse)
 // consecutive radix-2 stages are done per pass with a thread's eight elements in registers (the
 // same butterflies in the same order as one stage per pass), so a 512-point transform takes three
 // passes and barriers; indices come from shifts (P is a power of two).
+// three consecutive radix-2 stages st, st+1, st+2 on a thread's eight elements (stride h, offset
+// pos within the group)
+__device__ __forceinline__ void radix8(float2 (&x)[8], const float2* tw, int st, int pos, int h, int P, int inverse) {
+    const float2 w1 = tw_get(tw, pos * (P >> (st + 1)), inverse);
+#pragma unroll
+    for (int m = 0; m < 8; m += 2) {  // stage st: pairs (m, m+1)
+        const float2 c = cmul(x[m + 1], w1);
+        x[m + 1] = bfly_sub(x[m], c);
+        x[m] = bfly_add(x[m], c);
+    }
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {     // stage st+1: pairs (m, m+2) in groups of four
+        if (m & 2) continue;
+        const float2 w = tw_get(tw, (pos + (m & 1) * h) * (P >> (st + 2)), inverse);
+        const float2 c = cmul(x[m + 2], w);
+        x[m + 2] = bfly_sub(x[m], c);
+        x[m] = bfly_add(x[m], c);
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {     // stage st+2: pairs (m, m+4)
+        const float2 w = tw_get(tw, (pos + m * h) * (P >> (st + 3)), inverse);
+        const float2 c = cmul(x[m + 4], w);
+        x[m + 4] = bfly_sub(x[m], c);
+        x[m] = bfly_add(x[m], c);
+    }
+}
+
 template <int BS>
-__device__ __forceinline__ void fft_many(float2* Z, int q0, int nq, int P, int logP, const float2* tw, int inverse) {
-    int st = 0;
+__device__ __forceinline__ void fft_many(float2* Z, int q0, int nq, int P, int logP, const float2* tw, int inverse,
+                                         int st0 = 0) {
+    int st = st0;  // stages before st0 already done
     while (st < logP) {
         const int ns = min(3, logP - st);       // stages in this pass
         const int h = 1 << st;
@@ -145,28 +173,7 @@ __device__ __forceinline__ void fft_many(float2* Z, int q0, int nq, int P, int l
                 float2 x[8];
 #pragma unroll
                 for (int m = 0; m < 8; ++m) x[m] = Z[zp(zb + b0 + m * h)];
-                const float2 w1 = tw_get(tw, pos * (P >> (st + 1)), inverse);
-#pragma unroll
-                for (int m = 0; m < 8; m += 2) {  // stage st: pairs (m, m+1)
-                    const float2 c = cmul(x[m + 1], w1);
-                    x[m + 1] = bfly_sub(x[m], c);
-                    x[m] = bfly_add(x[m], c);
-                }
-#pragma unroll
-                for (int m = 0; m < 8; ++m) {     // stage st+1: pairs (m, m+2) in groups of four
-                    if (m & 2) continue;
-                    const float2 w = tw_get(tw, (pos + (m & 1) * h) * (P >> (st + 2)), inverse);
-                    const float2 c = cmul(x[m + 2], w);
-                    x[m + 2] = bfly_sub(x[m], c);
-                    x[m] = bfly_add(x[m], c);
-                }
-#pragma unroll
-                for (int m = 0; m < 4; ++m) {     // stage st+2: pairs (m, m+4)
-                    const float2 w = tw_get(tw, (pos + m * h) * (P >> (st + 3)), inverse);
-                    const float2 c = cmul(x[m + 4], w);
-                    x[m + 4] = bfly_sub(x[m], c);
-                    x[m] = bfly_add(x[m], c);
-                }
+                radix8(x, tw, st, pos, h, P, inverse);
 #pragma unroll
                 for (int m = 0; m < 8; ++m) Z[zp(zb + b0 + m * h)] = x[m];
             } else if (ns == 2) {
@@ -198,6 +205,43 @@ __device__ __forceinline__ void fft_many(float2* Z, int q0, int nq, int P, int l
     }
 }
 
+// The forward transform's first pass (stages 0-2, P >= 8) read straight from the slip rates: element
+// p of row pair q holds v - vpl at patch brev(p) of rows 2q (real part) and 2q + 1 (imaginary part),
+// zero beyond nx, so packing the rows in bit-reversed order and the pass's loads are one step (the
+// same values through the same butterflies). xin: v - vpl of every patch in shared memory, or null
+// to read the stage state.
+template <int BS>
+__device__ __forceinline__ void fft_first_from_rows(float2* Z, int nq, int P, int logP, const float2* tw,
+                                                    const float* xin, const double* __restrict__ v, double vpl,
+                                                    int nx, int nxi) {
+    const int lgi = logP - 3, items = nq << lgi;
+    for (int t = threadIdx.x; t < items; t += BS) {
+        const int q = t >> lgi, b0 = (t & ((1 << lgi) - 1)) * 8;
+        const int r0 = nx * (2 * q), r1 = nx * (2 * q + 1);
+        const bool odd = 2 * q + 1 < nxi;
+        float2 x[8];
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const int i = __brev(b0 + m) >> (32 - logP);
+            float re = 0.f, im = 0.f;
+            if (i < nx) {
+                if (xin) {
+                    re = xin[i + r0];
+                    if (odd) im = xin[i + r1];
+                } else {
+                    re = (float)(v[i + r0] - vpl);
+                    if (odd) im = (float)(v[i + r1] - vpl);
+                }
+            }
+            x[m] = make_float2(re, im);
+        }
+        radix8(x, tw, 0, 0, 1, P, 0);
+#pragma unroll
+        for (int m = 0; m < 8; ++m) Z[zp(q * P + b0 + m)] = x[m];
+    }
+    __syncthreads();
+}
+
 // fault-only RHS of one model: y (v, θ-or-ψ, δ) -> k. The traction rate is the rFFT convolution
 // of the reference (equation.jl:44-61) done in shared memory: two real rows per complex FFT,
 // a real per-frequency mixing (the symmetric circulant kernel has a real spectrum), two output
@@ -213,23 +257,28 @@ __device__ __forceinline__ void ens_rhs(const EnsModel& m, const EnsArgs& A, con
     const int nq = (nxi + 1) / 2;
     const double* v = y;
     const double* th = y + N;
-    // pack rows (2q, 2q+1) as real/imag, zero padded, in bit-reversed order
-    for (int t = threadIdx.x; t < nq * P; t += BS) {
-        const int q = t >> logP, i = t & (P - 1);
-        float re = 0.f, im = 0.f;
-        if (i < nx) {
-            if (xin) {
-                re = xin[i + nx * (2 * q)];
-                if (2 * q + 1 < nxi) im = xin[i + nx * (2 * q + 1)];
-            } else {
-                re = (float)(v[i + nx * (2 * q)] - m.vpl);
-                if (2 * q + 1 < nxi) im = (float)(v[i + nx * (2 * q + 1)] - m.vpl);
+    if (logP >= 3) {
+        fft_first_from_rows<BS>(S.Z, nq, P, logP, S.tw, xin, v, m.vpl, nx, nxi);
+        fft_many<BS>(S.Z, 0, nq, P, logP, S.tw, 0, 3);
+    } else {
+        // (P < 8) pack rows (2q, 2q+1) as real/imag, zero padded, in bit-reversed order
+        for (int t = threadIdx.x; t < nq * P; t += BS) {
+            const int q = t >> logP, i = t & (P - 1);
+            float re = 0.f, im = 0.f;
+            if (i < nx) {
+                if (xin) {
+                    re = xin[i + nx * (2 * q)];
+                    if (2 * q + 1 < nxi) im = xin[i + nx * (2 * q + 1)];
+                } else {
+                    re = (float)(v[i + nx * (2 * q)] - m.vpl);
+                    if (2 * q + 1 < nxi) im = (float)(v[i + nx * (2 * q + 1)] - m.vpl);
+                }
             }
+            S.Z[zp(q * P + (__brev(i) >> (32 - logP)))] = make_float2(re, im);
         }
-        S.Z[zp(q * P + (__brev(i) >> (32 - logP)))] = make_float2(re, im);
+        __syncthreads();
+        fft_many<BS>(S.Z, 0, nq, P, logP, S.tw, 0);
     }
-    __syncthreads();
-    fft_many<BS>(S.Z, 0, nq, P, logP, S.tw, 0);
     // Y_j[f] = sum_l G[j,l,f] X_l[f] (G real), the row spectra X taken straight from the transformed
     // pairs: X_{2q}[f] = (Z_q[f] + conj Z_q[P-f]) / 2, X_{2q+1}[f] = (Z_q[f] - conj Z_q[P-f]) / 2i.
     // Y is repacked (2q, 2q+1) as Y_2q + i Y_2q+1 with Hermitian fill, bit-reversed, into W for the
