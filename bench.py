@@ -57,6 +57,14 @@ NCU_TRAFFIC = {"fault-mantle-1000x2500-f64": 2044237000 + 2987264,
 # (5.39 GB) is above the capture size rule; its traffic is reported at the same ratio, since the
 # kernel streams every row once whatever the model's size.
 NCU_GEMV_TMA_SMALL = (520460000 + 3330000, 16128 * 16128 * 2)
+
+
+def gemv_tma_traffic(bytes_per_launch):
+    """(DRAM bytes of one k_gemv_tma launch of that many algorithmic bytes, how it was obtained)."""
+    tr, ab = NCU_GEMV_TMA_SMALL
+    return (round(bytes_per_launch * tr / ab),
+            f"k_gemv_tma's DRAM bytes per algorithmic byte in an ncu capture on the 1000 + 2500 model ({tr / ab:.4f}), "
+            "scaled to this launch's bytes (too large to capture)")
 # the headline ensemble: window of the horizon integrated by every arm (all 256 models)
 ENSEMBLE_WINDOW_YR = 8.0
 # the loading phase before the ensemble's first events (the earliest starts after 3 years)
@@ -475,12 +483,9 @@ def run_mixed_large(args):
                        "storage": f"{args.precision} with FP32 scale per 128x128 block, FP32 accumulate; FP32 Toeplitz (shared memory); FP64 friction, "
                                   f"{'ln-theta' if mixed_lt else 'theta'} state, error norm",
                        "l2": "inputs larger than L2"}, mx["ms"] / args.steps, args.precision)
-    tr, ab = NCU_GEMV_TMA_SMALL
-    traffic = round(mx["bytes"] * tr / ab) if args.precision in ("bf16", "f16") else None
+    traffic, tsrc = gemv_tma_traffic(mx["bytes"])
     line["roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                        "traffic": traffic,
-                        "traffic_source": "k_gemv_tma's DRAM bytes per algorithmic byte in an ncu capture on the "
-                                          "1000 + 2500 model, scaled to this launch's bytes (too large to capture)",
+                        "traffic": traffic, "traffic_source": tsrc,
                         "kernel": "k_gemv_tma (TMA cp.async.bulk.tensor pipeline) + k_prologue_mixed + k_fault_rows_smem",
                         "rhs_ms": mx["rhs_ms"], "bytes_per_launch": mx["bytes"]}
     line["fp64_gpu"] = {"value": years / (out["f64"]["ms"] / 1e3), "rhs_ms": out["f64"]["rhs_ms"], "rk_steps": out["f64"]["steps"]}
@@ -896,12 +901,9 @@ def run_headline(args):
             line["fault_mantle_4096x8000"] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
         mx = line.get("fault_mantle_4096x8000", {}).get("bf16")
         if mx:
-            tr, ab = NCU_GEMV_TMA_SMALL
+            traffic, tsrc = gemv_tma_traffic(mx["bytes_per_rhs"])
             line["roofline"] = {"bound": "hbm", "achieved": mx["achieved"], "peak": mx["peak"], "unit": "GB/s",
-                                "frac": mx["frac"], "traffic": round(mx["bytes_per_rhs"] * tr / ab),
-                                "traffic_source": "k_gemv_tma's DRAM bytes per algorithmic byte in an ncu capture on "
-                                                  f"the 1000 + 2500 model ({tr / ab:.4f}), scaled to this launch's "
-                                                  "bytes (too large to capture)",
+                                "frac": mx["frac"], "traffic": traffic, "traffic_source": tsrc,
                                 "kernel": mx["kernel"], "rhs_ms": mx["rhs_ms"],
                                 "bytes_per_launch": mx["bytes_per_rhs"], "peak_source": psrc,
                                 "note": "the 16-bit mantle GEMV of the mixed-precision form; the ensemble kernel "

@@ -31,3 +31,14 @@ def test_clock_samples_and_reasons(tmp_path):
     assert out["reasons"] == ["sw_power_cap"]
     assert not os.path.exists(c.path)
     assert bench.Clocks(0).stop()["reasons"] == ["nvidia-smi unavailable"]   # never started
+
+
+def test_gemv_traffic_scaled_from_the_small_capture():
+    """The default line's roofline traffic: DRAM bytes per algorithmic byte of the captured 1000 + 2500
+    launch (within 1 % of one: every row streamed once) times the 4096 + 8000 launch's bytes."""
+    import bench
+    tr, ab = bench.NCU_GEMV_TMA_SMALL
+    assert 1.0 <= tr / ab < 1.01
+    traffic, src = bench.gemv_tma_traffic(5394432000)
+    assert traffic == round(5394432000 * tr / ab) and 5394432000 < traffic < 1.01 * 5394432000
+    assert "scaled" in src
