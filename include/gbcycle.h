@@ -165,7 +165,7 @@ typedef struct gbc_solver_opts {
     double reltol, abstol;   /* error norm: RMS of err / (abstol + reltol * max(|u|, |u_new|)) */
     double dt0, dtmax, dtmin;
     long long maxiters;
-    int alg;                 /* GBC_ALG_*; 0 = Tsit5. Ensembles and the serving batch use Tsit5. */
+    int alg;                 /* GBC_ALG_TSIT5 (0) or GBC_ALG_VCABM5 (1), for every integrating call */
 } gbc_solver_opts;
 
 typedef struct gbc_solver_stats {
@@ -174,7 +174,8 @@ typedef struct gbc_solver_stats {
     int status;              /* 0 = reached t1, GBC_ESOLVER otherwise */
 } gbc_solver_stats;
 
-/* Tsit5 with PI step control from t0 to t1; u (flat, host) is overwritten with u(t1). */
+/* Tsit5 with PI step control or VCABM5 (opts->alg) from t0 to t1; u (flat, host) is overwritten
+ * with u(t1). */
 int gbc_integrate(gbc_model* m, double* u, double t0, double t1, const gbc_solver_opts* opts,
                   gbc_solver_stats* stats);
 /* gbc_integrate that also records the state history like the reference's wsolve callback

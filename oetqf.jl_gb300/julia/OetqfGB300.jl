@@ -213,4 +213,93 @@ function solve_gb300(s::GB300Sweep, U::Matrix{Float64}, t0, t1, alg; reltol=1e-6
     return out, st
 end
 
+"""
+Many fault-only models of uneven size, each with its own mesh, properties, initial state and time
+span, integrated in one persistent launch: per-model step control, large models split over
+thread-block clusters and re-planned onto larger clusters as others finish (`gbc_ensemble_*`). The
+batched counterpart of `solve(assemble(gf, p, u0, tspan), alg)` (src/BEM/equation.jl:81-89,
+src/io.jl:125-130) called on each model in turn.
+"""
+mutable struct GB300Ensemble
+    h::Ptr{Cvoid}
+    nmodels::Int
+end
+
+function GB300Ensemble(meshes::AbstractVector{<:RectOkadaMesh})
+    nx = Cint[mf.nx for mf in meshes]
+    nξ = Cint[mf.nξ for mf in meshes]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:gbc_ensemble_create, libgbc), Cint, (Cint, Ptr{Cint}, Ptr{Cint}, Ref{Ptr{Cvoid}}),
+                length(meshes), nx, nξ, h))
+    e = GB300Ensemble(h[], length(meshes))
+    finalizer(x -> ccall((:gbc_ensemble_destroy, libgbc), Cvoid, (Ptr{Cvoid},), x.h), e)
+    return e
+end
+
+"Model k's fault Green's function assembled on the device (stress_greens_function, src/BEM/GF.jl:31)."
+function assemble!(e::GB300Ensemble, k::Integer, mf::RectOkadaMesh, λ::Float64, μ::Float64;
+                   ftype=StrikeSlip(), nrept::Integer=2, buffer_ratio::Real=0)
+    ax, axi = pairs_rowmajor(mf.ax), pairs_rowmajor(mf.aξ)
+    GC.@preserve mf ax axi begin
+        m = GbcFaultMesh(mf.nx, mf.nξ, pointer(mf.x), pointer(mf.ξ), pointer(mf.y), pointer(mf.z),
+                         pointer(ax), pointer(axi), mf.Δx, mf.Δξ, mf.dep, mf.dip)
+        check(ccall((:gbc_ensemble_assemble, libgbc), Cint,
+                    (Ptr{Cvoid}, Cint, Ref{GbcFaultMesh}, Cdouble, Cdouble, Cint, Cint, Cdouble),
+                    e.h, k - 1, m, λ, μ, ftype isa StrikeSlip ? 0 : 1, nrept, buffer_ratio))
+    end
+end
+
+"Model k's fault Green's function from a host array: real (nx, nξ, nξ) or the rFFT form."
+function set_gf!(e::GB300Ensemble, k::Integer, gf::AbstractArray)
+    g = Array(gf)
+    check(ccall((:gbc_ensemble_set_gf, libgbc), Cint, (Ptr{Cvoid}, Cint, Cint, Ptr{Cvoid}),
+                e.h, k - 1, eltype(g) <: Complex ? 1 : 0, g))
+end
+
+function set_props!(e::GB300Ensemble, k::Integer, p::RateStateQuasiDynamicProperty)
+    check(ccall((:gbc_ensemble_set_fault_props, libgbc), Cint,
+                (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Cdouble, Cdouble, Cdouble, Cdouble),
+                e.h, k - 1, p.a, p.b, p.L, p.σ, p.η, p.vpl, p.f₀, p.v₀))
+end
+
+"""
+    solve_gb300(e, u0s, tspans, alg; reltol, abstol, dt, dtmax, maxiters, log_theta)
+
+Integrates model k from `tspans[k][1]` to `tspans[k][2]` starting from `u0s[k]` (an ArrayPartition
+(v, θ, δ) as `assemble` takes), all models in one batched call; returns the final states
+(ArrayPartitions like `u0s`) and one stats entry per model. `log_theta`: integrate ln θ in place of
+θ (the state handed back is θ either way); by default for Tsit5 only, since a multistep method on
+ln θ lands a tolerance-sized distance from the θ solution.
+"""
+function solve_gb300(e::GB300Ensemble, u0s::AbstractVector, tspans::AbstractVector, alg; reltol=1e-6, abstol=1e-8,
+                     dt=1e-8, dtmax=Inf, dtmin=1e-14, maxiters::Integer=10^9, log_theta::Bool=!(alg isa VCABM5))
+    n = e.nmodels
+    (length(u0s) == n && length(tspans) == n) || throw(DimensionMismatch("one state and one time span per model"))
+    code = alg isa VCABM5 ? Cint(1) : alg isa Tsit5 ? Cint(0) : throw(ArgumentError("VCABM5() or Tsit5()"))
+    check(ccall((:gbc_ensemble_set_log_theta, libgbc), Cint, (Ptr{Cvoid}, Cint), e.h, log_theta))
+    o = GbcSolverOpts(reltol, abstol, dt, isfinite(dtmax) ? dtmax : 1e300, dtmin, maxiters, code)
+    offset(k) = Int(ccall((:gbc_ensemble_state_offset, libgbc), Clonglong, (Ptr{Cvoid}, Cint), e.h, k - 1))
+    u = zeros(Int(ccall((:gbc_ensemble_state_len, libgbc), Clonglong, (Ptr{Cvoid},), e.h)))
+    for k in 1:n
+        flat = reduce(vcat, (vec(copy(x)) for x in u0s[k].x))
+        copyto!(u, offset(k) + 1, flat, 1, length(flat))
+    end
+    t0 = Float64[ts[1] for ts in tspans]
+    t1 = Float64[ts[2] for ts in tspans]
+    st = Vector{GbcStatsC}(undef, n)
+    rc = ccall((:gbc_ensemble_integrate, libgbc), Cint,
+               (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ref{GbcSolverOpts}, Ptr{GbcStatsC}),
+               e.h, u, t0, t1, o, st)
+    rc == 0 || rc == -5 || check(rc)
+    outs = map(1:n) do k
+        out = deepcopy(u0s[k])
+        off = offset(k)
+        for x in out.x
+            copyto!(x, 1, u, off + 1, length(x)); off += length(x)
+        end
+        out
+    end
+    return outs, st
+end
+
 end # module
