@@ -61,3 +61,17 @@ def test_failure_injection_hook_checks_its_mode_before_any_device_use():
     from oetqf_gb300 import _capi as C
     assert C.lib().gbc_debug_pipeline_fault(7) == -1
     assert "mode" in C.last_error()
+
+
+def test_julia_binding_calls_only_declared_symbols():
+    """The Julia glue (no Julia toolchain here) binds only entry points the header declares and the
+    library exports."""
+    from oetqf_gb300 import _capi as C
+    src = open(os.path.join(ROOT, "oetqf.jl_gb300", "julia", "OetqfGB300.jl")).read()
+    called = set(re.findall(r"ccall\(\(:(gbc_[a-z0-9_]+), libgbc\)", src))
+    assert {"gbc_rhs", "gbc_integrate", "gbc_sweep_integrate", "gbc_ensemble_integrate"} <= called
+    declared = set(_declared())
+    L = C.lib()
+    for n in called:
+        assert n in declared, n
+        assert hasattr(L, n), n
