@@ -886,8 +886,9 @@ int ens_csize(int N, int maxc, int boost) {
 // Predicted microseconds per VCABM5 step of an N-patch model on a cluster of c CTAs of 512 threads:
 // a fixed part (step control and barriers), the model's patches spread over the cluster (FFT
 // convolution, friction, error norm) and the cluster's exchanges. A fit to single-model timings on
-// a GB300 (N = 400 to 1960, c = 1 to 16, within 10 %); it only ranks the models when they are
-// planned onto clusters.
+// a GB300 (N = 400 to 1960, c = 1 to 16, within 10 %) of an earlier version of the kernel, whose
+// steps were ~1.5x longer throughout; it only ranks the models and the gains of larger clusters
+// when they are planned, which the uniform speed-up leaves in the same order.
 double ens_step_us(int N, int c) {
     int lg = 0;
     while ((1 << lg) < c) ++lg;
