@@ -1372,8 +1372,9 @@ int gbc_ensemble_set_regroup(gbc_ensemble* e, int on) {
 
 int gbc_ensemble_plan_clusters(int n, const int* npatch, const int* done, const double* steps_left,
                                const int* capacity, int* sizes) {
-    if (n < 0 || (n > 0 && (!npatch || !done || !steps_left || !capacity || !sizes)))
+    if (n < 0 || !capacity || (n > 0 && (!npatch || !done || !steps_left || !sizes)))
         return fail(GBC_EINVAL, "null argument");
+    if (n == 0) return 0;
     double cap[kEnsGroups];
     for (int g = 0; g < kEnsGroups; ++g) {
         if (capacity[g] < 0) return fail(GBC_EINVAL, "negative cluster capacity");

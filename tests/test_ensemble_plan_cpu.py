@@ -77,3 +77,17 @@ def test_invalid_capacity_rejected():
         Ensemble.plan_clusters([1000], [0], [1.0], [304, -1, 36, 15, 7])
     with pytest.raises(ValueError):
         Ensemble.plan_clusters([1000], [0], [1.0], [304, 76])
+
+
+def test_plan_entry_point_checks_its_arguments():
+    import ctypes
+    from oetqf_gb300 import _capi as C
+    L = C.lib()
+    ip = ctypes.POINTER(ctypes.c_int)
+    null_i = ctypes.cast(None, ip)
+    null_d = ctypes.cast(None, ctypes.POINTER(ctypes.c_double))
+    assert L.gbc_ensemble_plan_clusters(-1, null_i, null_i, null_d, null_i, null_i) < 0
+    assert L.gbc_ensemble_plan_clusters(2, null_i, null_i, null_d, null_i, null_i) < 0
+    assert L.gbc_ensemble_plan_clusters(0, null_i, null_i, null_d, null_i, null_i) < 0  # no capacities
+    cap = (ctypes.c_int * 5)(304, 76, 36, 15, 7)
+    assert L.gbc_ensemble_plan_clusters(0, null_i, null_i, null_d, cap, null_i) == 0  # nothing to plan
