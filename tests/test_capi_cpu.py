@@ -75,3 +75,34 @@ def test_julia_binding_calls_only_declared_symbols():
     for n in called:
         assert n in declared, n
         assert hasattr(L, n), n
+
+
+_NULL_CALLS = r'''
+import ctypes, sys
+sys.path[:0] = [sys.argv[1]]
+from oetqf_gb300 import _capi as C
+from oetqf_gb300 import serving
+L = C.lib()
+serving._sigs()
+zero = {ctypes.c_int: 0, ctypes.c_longlong: 0, ctypes.c_size_t: 0, ctypes.c_long: 0, ctypes.c_double: 0.0,
+        ctypes.c_float: 0.0}
+for name in sys.argv[2:]:
+    f = getattr(L, name)
+    if f.argtypes is None:
+        continue
+    print(name, flush=True)
+    f(*[zero.get(a) for a in f.argtypes])
+print("done", flush=True)
+'''
+
+
+def test_every_entry_point_survives_null_and_zero_arguments():
+    """Each declared entry point called with null pointers and zero sizes returns (an error code, or
+    nothing for the destroy functions) instead of crashing: arguments are checked before use."""
+    import subprocess
+    import sys
+    names = _declared()
+    p = subprocess.run([sys.executable, "-c", _NULL_CALLS, os.path.join(ROOT, "oetqf.jl_gb300"), *names],
+                       capture_output=True, text=True, timeout=300)
+    lines = p.stdout.split()
+    assert p.returncode == 0 and lines[-1] == "done", f"crashed after {lines[-1:]}: {p.stderr[-500:]}"
