@@ -98,7 +98,10 @@ print("done", flush=True)
 
 def test_every_entry_point_survives_null_and_zero_arguments():
     """Each declared entry point called with null pointers and zero sizes returns (an error code, or
-    nothing for the destroy functions) instead of crashing: arguments are checked before use."""
+    nothing for the destroy functions) instead of crashing: arguments are checked before use. Host
+    only: where a GPU is present the calls could reach device work, so the probe does not run."""
+    if _has_gpu():
+        pytest.skip("host-only probe of the argument checks")
     import subprocess
     import sys
     names = _declared()
