@@ -296,3 +296,17 @@ def test_fft_convolution_variant_equals_the_direct_transform(oracle):
     for (u1, _), u2, s2 in zip(seq, fast, st):
         assert s2.status == 0
         assert np.abs(u1 - u2).max() <= 1e-9 * np.abs(u1).max()
+
+
+def test_fft_convolution_variant_at_the_smallest_shapes(oracle):
+    """The FFT variant at transform lengths 2 to 16 (nx = 1 to 4; one to five depth rows, odd and
+    even) equals the direct transforms to round-off."""
+    from oetqf_gb300 import RateStateQuasiDynamicProperty, gen_mesh
+    for nx, nxi in [(1, 1), (1, 2), (2, 1), (2, 3), (3, 2), (4, 5)]:
+        mf = gen_mesh("RectOkada", 1e3 * nx, 1e3 * nxi, 1e3, 1e3, 90.0)
+        o = np.ones((nx, nxi))
+        pf = RateStateQuasiDynamicProperty(0.015 * o, 0.019 * o, 0.012 * o, 5e7 * o, 4.9e6, 1e-9, 0.6, 1e-6)
+        om = oracle.OracleModel(oracle.gf_ff(mf, 3e10, 3e10, fourier=True), pf)
+        v = 1e-9 * np.exp(np.random.default_rng(nx * 7 + nxi).uniform(-2, 8, nx * nxi))
+        a, b = om.dtau_dt(v), oracle.dtau_dt_fft(om, v)
+        assert np.abs(a - b).max() <= 1e-14 * np.abs(a).max()
